@@ -1,0 +1,189 @@
+/*
+ * synchrowords GB300 — C ABI of the GPU exact shortest-reset-word search.
+ *
+ * Drop-in boundary for SynchroLib 1.1.0's plugin entry
+ *   extern "C" void run(const std::string& aut_encoded,
+ *                       const std::vector<std::string>& algorithms,
+ *                       AlgoResult& result, Logger::LogLevel)
+ * (jit/jitmain.cpp:11-49), which passes C++ objects and needs N, K at compile
+ * time.  This ABI takes plain pointers and sizes, dispatches on the runtime
+ * number of states n (1..512) and alphabet size k (1..16), returns status
+ * codes (nothing throws across it) and keeps device buffers in an opaque
+ * context between calls.
+ *
+ * Automaton layout (as the reference, synchrolib/data_structures/automaton/
+ * automaton.hpp:14-33 and app/io.hpp:136-159): delta[q*k + a] is the state
+ * reached from q by letter a, 0 <= delta[.] < n.
+ *
+ * Host bitset layout used by the kernel-level entry points (as the
+ * reference's Subset<N>, synchrolib/data_structures/subset.hpp:11-26): a set
+ * is ceil(n/64) uint64 words, state q is bit q%64 of word q/64, bits >= n are 0.
+ */
+#ifndef SYNCHROWORDS_H
+#define SYNCHROWORDS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SW_OK 0
+#define SW_ERR_INVALID_ARGUMENT (-1) /* bad pointer, size or automaton entry */
+#define SW_ERR_CONFIG (-2)           /* plan JSON / expression error (app/jit.hpp:61-83 exit 4) */
+#define SW_ERR_CUDA (-3)             /* CUDA runtime error (reference: checkCudaErrors + exit) */
+#define SW_ERR_NO_DEVICE (-4)        /* no CUDA device: this library has no CPU fallback */
+#define SW_ERR_UNSUPPORTED (-5)      /* algorithm outside this library's scope */
+#define SW_ERR_INTERNAL (-6)         /* internal check failed (e.g. word verification) */
+#define SW_ERR_CAPACITY (-7)         /* caller buffer too small */
+
+#define SW_MAX_STATES 512
+#define SW_MAX_LETTERS 16
+#define SW_MAX_ALGORITHMS 16
+#define SW_NAME_LEN 16
+
+/* ---- plan (the reference's JSON config, evaluated for one (n, k)) -------- */
+typedef enum {
+  SW_ALGO_EXACT = 1,    /* synchrolib/algorithm/exact/ */
+  SW_ALGO_BEAM = 2,     /* synchrolib/algorithm/beam/ */
+  SW_ALGO_BRUTE = 3,    /* synchrolib/algorithm/brute/ (outside this library's scope) */
+  SW_ALGO_EPPSTEIN = 4, /* synchrolib/algorithm/eppstein/ (outside this library's scope) */
+  SW_ALGO_REDUCE = 5    /* synchrolib/algorithm/reduce/ (outside this library's scope) */
+} sw_algo_kind;
+
+/* Evaluated Exact defines (synchrolib/algorithm/exact/config.hpp:24-46). */
+typedef struct {
+  int32_t dfs;                  /* "dfs" (default true) */
+  int32_t dfs_shortcut;         /* "dfs_shortcut" (default true) */
+  int32_t strict_memory_limit;  /* "strict_memory_limit" (default false) */
+  uint64_t max_memory_mb;       /* "max_memory_mb" (default 2048): device budget of the lists */
+  uint64_t dfs_min_list_size;   /* "dfs_min_list_size" (default 10000) */
+  uint64_t bfs_small_list_size; /* "bfs_small_list_size" (default AUT_N * 16) */
+} sw_exact_config;
+
+/* Evaluated Beam defines (synchrolib/algorithm/beam/config.hpp:23-44). */
+typedef struct {
+  uint64_t beam_size;      /* "beam_size" (default std::log2(AUT_N)) */
+  int32_t dynamic;         /* "dynamic" (default false) */
+  uint64_t min_beam_size;  /* "min_beam_size" (default AUT_N * std::log2(AUT_N)) */
+  uint64_t max_beam_size;  /* "max_beam_size" (default AUT_N * AUT_N * std::log2(AUT_N)) */
+  double beam_exact_ratio; /* "beam_exact_ratio" (default 0.01) */
+  int64_t max_iter;        /* "max_iter" (default -1) */
+  int32_t presort_indeg;   /* "presort": 0 = "none", 1 = "indeg" */
+} sw_beam_config;
+
+typedef struct {
+  int32_t kind; /* sw_algo_kind */
+  char name[SW_NAME_LEN];
+  sw_exact_config exact;
+  sw_beam_config beam;
+} sw_algorithm;
+
+/* Global plan keys (app/jit.hpp:112-141, docs/config.md:15-27). */
+typedef struct {
+  uint64_t upper_bound;       /* "upper_bound" (default 1ULL*AUT_N*AUT_N*AUT_N/6) */
+  uint32_t threads;           /* "threads" (1..64; host threads of the CPU reference only) */
+  int32_t gpu;                /* "gpu" (accepted; this library always runs on the GPU) */
+  uint64_t gpu_max_memory_mb; /* "gpu_max_memory_mb" (default 2048) */
+  uint32_t n_algorithms;
+  sw_algorithm algorithms[SW_MAX_ALGORITHMS];
+} sw_plan;
+
+/* ---- result (synchrolib/algorithm/algorithm.hpp:19-42) ------------------ */
+typedef struct {
+  char name[SW_NAME_LEN];
+  uint64_t ms;
+} sw_algo_run;
+
+typedef struct {
+  uint64_t subsets_expanded;  /* children produced by layer expansion */
+  uint64_t subsets_kept;      /* sets that survived dedup + dominance */
+  uint64_t trie_queries;      /* subset queries issued against a radix tree */
+  uint64_t logical_pairs;     /* sum over queries of the queried list size (|S| per query) */
+  uint64_t meet_pairs;        /* logical (F, B) pairs covered by meet checks */
+  uint64_t bfs_steps;         /* forward layers */
+  uint64_t ibfs_steps;        /* inverse layers */
+  uint64_t dfs_sets;          /* sets generated in the memory-bounded inverse DFS phase */
+  uint64_t kernel_launches;   /* device kernels launched by the solve */
+  double device_ms;           /* wall time of the solve spent in the GPU search */
+} sw_stats;
+
+typedef struct {
+  int32_t non_synchro;
+  uint64_t mlsw_lower_bound;
+  uint64_t mlsw_upper_bound;
+  int32_t has_word;       /* 1 if word[0..word_len) is a verified reset word */
+  uint32_t word_len;
+  uint32_t* word;         /* caller buffer, may be NULL */
+  uint32_t word_capacity; /* entries available in `word` */
+  uint32_t n_runs;
+  sw_algo_run runs[SW_MAX_ALGORITHMS];
+  sw_stats stats;
+} sw_result;
+
+typedef struct sw_context sw_context;
+
+/* ---- library ------------------------------------------------------------ */
+const char* sw_version(void);
+/* Message of the last failed call on this thread ("" if none). */
+const char* sw_last_error(void);
+
+/* Parse a plan (the reference's config JSON, docs/config.md) and evaluate its
+ * expressions for an automaton with n states and k letters.  Replaces
+ * AlgoConfig::get_substs + the JIT's compile-time evaluation
+ * (synchrolib/algorithm/config.hpp:57-60, app/jit.hpp:96-141). */
+int sw_plan_from_json(const char* json, uint32_t n, uint32_t k, sw_plan* out);
+
+/* Evaluate one C++ config expression (AUT_N = n, AUT_K = k) as the reference's
+ * compiler would and convert it to uint64 / double.  For tests and tools. */
+int sw_eval_expression(const char* expr, uint32_t n, uint32_t k, uint64_t* as_u64, double* as_double);
+
+/* Context = one CUDA device + persistent device buffers.  Not thread-safe:
+ * use one context per host thread (the reference is single-caller too). */
+int sw_context_create(int device, sw_context** out);
+void sw_context_destroy(sw_context* ctx);
+
+/* Run every algorithm of `plan` in order on one automaton, as the reference's
+ * run() does (jit/jitmain.cpp:11-49): bounds start at
+ * [0, min(upper_bound, UINT64_MAX)], each algorithm may tighten them, and
+ * per-algorithm milliseconds are recorded.  `result->word` (if non-NULL)
+ * receives a reset word of length mlsw_upper_bound when one was found and
+ * verified (the reference's Exact returns no word; this one does). */
+int sw_solve(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const sw_plan* plan,
+             sw_result* result);
+
+/* Same as sw_solve with the plan given as JSON text (evaluated for this n, k). */
+int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const char* plan_json,
+                  sw_result* result);
+
+/* ---- kernel-level entry points (host buffers, reference bitset layout) ---
+ * These are the device operations the reference offloads, exposed for parity
+ * tests and for callers that drive their own search. */
+
+/* Image (inverse = 0) or preimage-union (inverse = 1) of `count` sets under
+ * one letter.  Replaces preprocessed_transition_kernel
+ * (synchrolib/data_structures/cuda/preprocessed_transition_kernel.cu:54-88)
+ * and PreprocessedTransition::apply (preprocessed_transitions.cpp:56-93). */
+int sw_apply_transition(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, uint32_t letter,
+                        int32_t inverse, const uint64_t* from, uint64_t* to, uint64_t count);
+
+/* results[i] = 1 if some sets[j] ⊆ checks[i] (sets[j] ⊊ checks[i] when
+ * proper), else 0.  Replaces SubsetsImplicitTrieKernel::run /
+ * subsets_trie_kernel_impl_v2 and the proper variant
+ * (synchrolib/data_structures/cuda/subsets_implicit_trie_kernel.cu:13-92,
+ * 183-223) and SubsetsImplicitTrie::check_contains_subset
+ * (synchrolib/data_structures/subsets_implicit_trie.hpp:29-44). */
+int sw_subsets_check(sw_context* ctx, uint32_t n, const uint64_t* sets, uint64_t set_count, const uint64_t* checks,
+                     uint64_t check_count, int32_t proper, uint8_t* results);
+
+/* Sort (in the reference's order, subset.hpp:71-77) and deduplicate `count`
+ * sets in place; *out_count receives the number kept.  Replaces
+ * sort_keep_unique (synchrolib/utils/vector.hpp:13-27). */
+int sw_sort_unique(sw_context* ctx, uint32_t n, uint64_t* sets, uint64_t count, uint64_t* out_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SYNCHROWORDS_H */

@@ -1,0 +1,260 @@
+"""synchrowords GB300: GPU exact shortest-reset-word search (SynchroLib drop-in).
+
+Python front end over the C ABI in ``include/synchrowords.h``.  It mirrors the
+reference's plugin interface (jit/jitmain.cpp:11-49): a plan (the reference's
+config JSON) is evaluated for one automaton and its algorithms run in order on
+the GPU, producing an ``AlgoResult``-like record (bounds, per-algorithm
+milliseconds and, new here, a verified reset word).
+
+The library has no CPU path: loading fails loudly when the compiled library
+is missing, and creating a context fails when no CUDA device is present.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+__all__ = ["Context", "Result", "SynchroError", "read_automata", "format_result", "plan_from_json",
+           "eval_expression", "library_path", "load_library", "MAX_STATES", "MAX_LETTERS"]
+
+PKG = Path(__file__).resolve().parent
+MAX_STATES = 512
+MAX_LETTERS = 16
+NAME_LEN = 16
+MAX_ALGOS = 16
+
+
+def library_path() -> Path:
+    return PKG / "_build" / "libsynchrowords.so"
+
+
+class SynchroError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+# ---- ctypes mirrors of include/synchrowords.h --------------------------------
+class _ExactCfg(ctypes.Structure):
+    _fields_ = [("dfs", ctypes.c_int32), ("dfs_shortcut", ctypes.c_int32), ("strict_memory_limit", ctypes.c_int32),
+                ("max_memory_mb", ctypes.c_uint64), ("dfs_min_list_size", ctypes.c_uint64),
+                ("bfs_small_list_size", ctypes.c_uint64)]
+
+
+class _BeamCfg(ctypes.Structure):
+    _fields_ = [("beam_size", ctypes.c_uint64), ("dynamic", ctypes.c_int32), ("min_beam_size", ctypes.c_uint64),
+                ("max_beam_size", ctypes.c_uint64), ("beam_exact_ratio", ctypes.c_double),
+                ("max_iter", ctypes.c_int64), ("presort_indeg", ctypes.c_int32)]
+
+
+class _Algo(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("name", ctypes.c_char * NAME_LEN), ("exact", _ExactCfg),
+                ("beam", _BeamCfg)]
+
+
+class _Plan(ctypes.Structure):
+    _fields_ = [("upper_bound", ctypes.c_uint64), ("threads", ctypes.c_uint32), ("gpu", ctypes.c_int32),
+                ("gpu_max_memory_mb", ctypes.c_uint64), ("n_algorithms", ctypes.c_uint32),
+                ("algorithms", _Algo * MAX_ALGOS)]
+
+
+class _Run(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * NAME_LEN), ("ms", ctypes.c_uint64)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("subsets_expanded", ctypes.c_uint64), ("subsets_kept", ctypes.c_uint64),
+                ("trie_queries", ctypes.c_uint64), ("logical_pairs", ctypes.c_uint64),
+                ("meet_pairs", ctypes.c_uint64), ("bfs_steps", ctypes.c_uint64), ("ibfs_steps", ctypes.c_uint64),
+                ("dfs_sets", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("device_ms", ctypes.c_double)]
+
+
+class _Result(ctypes.Structure):
+    _fields_ = [("non_synchro", ctypes.c_int32), ("mlsw_lower_bound", ctypes.c_uint64),
+                ("mlsw_upper_bound", ctypes.c_uint64), ("has_word", ctypes.c_int32), ("word_len", ctypes.c_uint32),
+                ("word", ctypes.POINTER(ctypes.c_uint32)), ("word_capacity", ctypes.c_uint32),
+                ("n_runs", ctypes.c_uint32), ("runs", _Run * MAX_ALGOS), ("stats", _Stats)]
+
+
+_lib = None
+
+_U32P = ctypes.POINTER(ctypes.c_uint32)
+_U64P = ctypes.POINTER(ctypes.c_uint64)
+
+
+def load_library():
+    """Load the compiled library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not path.exists():
+        raise ImportError(f"synchrowords_gb300 native library not built ({path}); "
+                          "run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = ctypes.CDLL(str(path))
+    lib.sw_version.restype = ctypes.c_char_p
+    lib.sw_last_error.restype = ctypes.c_char_p
+    lib.sw_plan_from_json.argtypes = [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_Plan)]
+    lib.sw_eval_expression.argtypes = [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint32, _U64P,
+                                       ctypes.POINTER(ctypes.c_double)]
+    lib.sw_context_create.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+    lib.sw_context_destroy.argtypes = [ctypes.c_void_p]
+    lib.sw_solve.argtypes = [ctypes.c_void_p, _U32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_Plan),
+                             ctypes.POINTER(_Result)]
+    lib.sw_solve_json.argtypes = [ctypes.c_void_p, _U32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_char_p,
+                                  ctypes.POINTER(_Result)]
+    lib.sw_apply_transition.argtypes = [ctypes.c_void_p, _U32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_int32, _U64P, _U64P, ctypes.c_uint64]
+    lib.sw_subsets_check.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P,
+                                     ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint8)]
+    lib.sw_sort_unique.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P]
+    _lib = lib
+    return lib
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise SynchroError(rc, load_library().sw_last_error().decode())
+
+
+def _u32(a: Sequence[int]) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.uint32))
+
+
+def eval_expression(expr: str, n: int, k: int) -> Tuple[int, float]:
+    """(uint64 value, double value) of a config expression with AUT_N = n, AUT_K = k."""
+    u = ctypes.c_uint64()
+    d = ctypes.c_double()
+    _check(load_library().sw_eval_expression(expr.encode(), n, k, ctypes.byref(u), ctypes.byref(d)))
+    return u.value, d.value
+
+
+def plan_from_json(text: str, n: int, k: int) -> dict:
+    """Evaluated plan as a dict (the library's view of the reference config)."""
+    p = _Plan()
+    _check(load_library().sw_plan_from_json(text.encode(), n, k, ctypes.byref(p)))
+    algos = []
+    for i in range(p.n_algorithms):
+        a = p.algorithms[i]
+        d = {"kind": a.kind, "name": a.name.decode()}
+        if a.kind == 1:
+            d.update({f: getattr(a.exact, f) for f, _ in _ExactCfg._fields_})
+        elif a.kind == 2:
+            d.update({f: getattr(a.beam, f) for f, _ in _BeamCfg._fields_})
+        algos.append(d)
+    return {"upper_bound": p.upper_bound, "threads": p.threads, "gpu": p.gpu,
+            "gpu_max_memory_mb": p.gpu_max_memory_mb, "algorithms": algos}
+
+
+@dataclass
+class Result:
+    """AlgoResult (synchrolib/algorithm/algorithm.hpp:19-42) plus statistics."""
+    non_synchro: bool
+    lower: int
+    upper: int
+    word: Optional[List[int]]
+    runs: List[Tuple[str, int]]
+    stats: dict = field(default_factory=dict)
+
+
+class Context:
+    """One CUDA device with persistent buffers (not thread-safe)."""
+
+    def __init__(self, device: int = 0):
+        self._lib = load_library()
+        self._h = ctypes.c_void_p()
+        _check(self._lib.sw_context_create(device, ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if self._h:
+            self._lib.sw_context_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def solve(self, delta: Sequence[int], n: int, k: int, plan_json: str) -> Result:
+        d = _u32(delta)
+        if d.size != n * k:
+            raise ValueError("delta must have n*k entries")
+        cap = max(1 << 16, 4 * n * n)
+        buf = np.zeros(cap, dtype=np.uint32)
+        r = _Result()
+        r.word = buf.ctypes.data_as(_U32P)
+        r.word_capacity = cap
+        _check(self._lib.sw_solve_json(self._h, d.ctypes.data_as(_U32P), n, k, plan_json.encode(), ctypes.byref(r)))
+        word = buf[: r.word_len].tolist() if r.has_word else None
+        runs = [(r.runs[i].name.decode(), r.runs[i].ms) for i in range(r.n_runs)]
+        stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
+        return Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats)
+
+    # ---- kernel-level entry points (reference bitset layout) ----
+    def apply_transition(self, delta, n: int, k: int, letter: int, inverse: bool, sets: np.ndarray) -> np.ndarray:
+        d = _u32(delta)
+        s = np.ascontiguousarray(sets, dtype=np.uint64)
+        out = np.zeros_like(s)
+        cnt = s.shape[0] if s.ndim > 1 else (s.size // max(1, (n + 63) // 64))
+        _check(self._lib.sw_apply_transition(self._h, d.ctypes.data_as(_U32P), n, k, letter, int(inverse),
+                                             s.ctypes.data_as(_U64P), out.ctypes.data_as(_U64P), cnt))
+        return out
+
+    def subsets_check(self, n: int, sets: np.ndarray, checks: np.ndarray, proper: bool = False) -> np.ndarray:
+        s = np.ascontiguousarray(sets, dtype=np.uint64)
+        c = np.ascontiguousarray(checks, dtype=np.uint64)
+        rw = (n + 63) // 64
+        ns, nc = s.size // rw, c.size // rw
+        out = np.zeros(nc, dtype=np.uint8)
+        _check(self._lib.sw_subsets_check(self._h, n, s.ctypes.data_as(_U64P), ns, c.ctypes.data_as(_U64P), nc,
+                                          int(proper), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))))
+        return out
+
+    def sort_unique(self, n: int, sets: np.ndarray) -> np.ndarray:
+        rw = (n + 63) // 64
+        s = np.ascontiguousarray(sets, dtype=np.uint64).copy()
+        cnt = ctypes.c_uint64()
+        _check(self._lib.sw_sort_unique(self._h, n, s.ctypes.data_as(_U64P), s.size // rw, ctypes.byref(cnt)))
+        return s.reshape(-1, rw)[: cnt.value]
+
+
+def read_automata(path) -> List[Tuple[int, int, List[int]]]:
+    """Automata in the reference's input format (app/io.hpp:136-159): "K N" then N*K ints."""
+    toks = Path(path).read_text().split()
+    out = []
+    i = 0
+    while i + 1 < len(toks):
+        k, n = int(toks[i]), int(toks[i + 1])
+        i += 2
+        if n <= 0 or k <= 0:
+            raise ValueError("N and K must be greater than 0")
+        d = [int(x) for x in toks[i:i + n * k]]
+        if len(d) != n * k:
+            raise ValueError(f"Expected {n * k} integers, found {len(d)}")
+        if any(x < 0 or x >= n for x in d):
+            raise ValueError(f"Expected integer in range [0, {n - 1}]")
+        i += n * k
+        out.append((n, k, d))
+    return out
+
+
+def format_result(index: int, r: Result) -> str:
+    """Output line of app/io.hpp:176-224: `ID: [lb, ub] ((Algo, ms), ...) {w...}`."""
+    if r.non_synchro:
+        return f"{index}: NON SYNCHRO"
+    runs = ", ".join(f"({n}, {ms})" for n, ms in r.runs)
+    s = f"{index}: [{r.lower}, {r.upper}] ({runs})"
+    if r.word is not None:
+        s += " {" + " ".join(map(str, r.word)) + "}"
+    return s

@@ -1,0 +1,108 @@
+// Shared definitions for the synchrowords GB300 library (host + device).
+//
+// Set layout on the device ("MSB-first rows"): a set of n states is a row of
+// W 64-bit words (W = 1, 2, 4 or 8: 64/128/256/512-bit classes); state q is
+// bit (63 - q % 64) of word q / 64.  With this layout the numeric order of
+// rows (word 0 most significant) is the reference's lexicographic order of
+// sets (state 0 most significant, synchrolib/data_structures/subset.hpp:71-77),
+// so one radix sort of raw words yields the order the prefix trie needs.
+// Unused tail bits are zero.  Rows are 8*W bytes and 16-byte aligned for W>=2
+// so warps move them as uint4.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+
+namespace sw {
+
+using u64 = unsigned long long;
+using u32 = uint32_t;
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+#define SW_CUDA(call)                                                                      \
+  do {                                                                                     \
+    cudaError_t _e = (call);                                                               \
+    if (_e != cudaSuccess)                                                                 \
+      throw ::sw::CudaError(std::string(#call) + " failed: " + cudaGetErrorString(_e) +  \
+                            " at " + __FILE__ + ":" + std::to_string(__LINE__));           \
+  } while (0)
+
+#define SW_LAUNCH_CHECK() SW_CUDA(cudaGetLastError())
+
+constexpr int kMaxStates = 512;
+constexpr int kMaxLetters = 16;
+
+inline int words_for(int n) {
+  int w = (n + 63) / 64;
+  return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : 8;
+}
+
+// Device-side bit helpers for the MSB-first layout.
+__host__ __device__ inline u64 state_bit(int q) { return 1ULL << (63 - (q & 63)); }
+__host__ __device__ inline int state_word(int q) { return q >> 6; }
+
+// Mask of valid bits of word `w` for an n-state set.
+__host__ __device__ inline u64 valid_mask(int n, int w) {
+  int lo = w * 64;
+  if (n >= lo + 64) return ~0ULL;
+  if (n <= lo) return 0ULL;
+  int bits = n - lo;
+  return ~0ULL << (64 - bits);
+}
+
+// Grow-only device buffer (the context keeps them across steps and solves,
+// so a solve performs no per-step cudaMalloc).
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  void reserve(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) SW_CUDA(cudaFree(p));
+    p = nullptr;
+    size_t want = bytes + bytes / 4 + 256;
+    SW_CUDA(cudaMalloc(&p, want));
+    cap = want;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// Pinned host staging for small readbacks.
+struct HostPinned {
+  void* p = nullptr;
+  size_t cap = 0;
+  ~HostPinned() {
+    if (p) cudaFreeHost(p);
+  }
+  void reserve(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) SW_CUDA(cudaFreeHost(p));
+    SW_CUDA(cudaMallocHost(&p, bytes));
+    cap = bytes;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+}  // namespace sw

@@ -1,0 +1,586 @@
+// Host driver of the GPU exact search and beam (see exact.hpp).
+//
+// Exact (synchrolib/algorithm/exact/exact.cpp:37-97, meet_in_the_middle.cpp:58-344):
+// two frontiers live on the device,
+//   F: forward images  delta(Q, w), seeded with {Q}           (exact.cpp:130-146)
+//   B: inverse preimages, seeded with sink singletons whose
+//      state has some letter of in-degree > 1                (exact.cpp:149-164)
+// B is stored as complements: the preimage of a complement is the complement
+// of the preimage, so the same expansion, dedup and dominance code serves both
+// sides.  One step expands the smaller side (meet_in_the_middle.cpp:355-358),
+// sorts and deduplicates the children, drops every child that has a visited
+// set inside it or a proper subset in its own layer
+// (meet_in_the_middle.cpp:179-344 on complements for B), and then asks
+// whether some F is disjoint from some B-complement (F ⊆ B,
+// meet_in_the_middle.cpp:90).  Each kept child records (letter, parent) so the
+// meeting pair yields a word, which is verified on the host before it is
+// returned.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+#include <string>
+
+#include "exact.hpp"
+#include "kernels.cuh"
+
+namespace sw {
+
+namespace {
+
+struct Layer {
+  DevBuf origin;        // per kept set: child position a*parent_count + parent
+  u32 count = 0;
+  u32 parent_count = 0;
+};
+
+struct Side {
+  DevBuf rows, rows_alt;
+  u32 count = 0;
+  DevBuf vis, vis_alt;
+  u32 vis_count = 0;
+  DevBuf vis_gamma, vis_split;
+  DevBuf gamma, split;  // tree over `rows` (kept for F only)
+  std::vector<std::unique_ptr<Layer>> layers;
+  std::vector<u64> seed_states;  // backward side: the state of each seed row
+  void reset() {
+    count = vis_count = 0;
+    layers.clear();
+    seed_states.clear();
+  }
+};
+
+}  // namespace
+
+class Engine {
+ public:
+  explicit Engine(int device) {
+    SW_CUDA(cudaSetDevice(device));
+    SW_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    pinned.reserve(4096);
+    SW_CUDA(cudaMalloc(&d_misc, 64 * sizeof(u32)));
+  }
+  ~Engine() {
+    if (d_misc) cudaFree(d_misc);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  cudaStream_t stream = nullptr;
+  HostPinned pinned;
+  u32* d_misc = nullptr;  // [0..3] witness, [8] scan total
+  // tables
+  DevBuf t_delta, t_beg, t_src;
+  TransTables tables;
+  // scratch
+  DevBuf ch_rows, ch_vals, alt_rows, alt_vals, uq_rows, uq_vals, new_vals;
+  DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt;
+  Side F, B;
+  sw_stats* st = nullptr;
+
+  void upload_tables(const Automaton& A) {
+    HostTables h = build_tables(A);
+    t_delta.reserve(h.delta.size() * 2);
+    t_beg.reserve(h.inv_beg.size() * 2);
+    t_src.reserve(h.inv_src.size() * 2);
+    SW_CUDA(cudaMemcpyAsync(t_delta.p, h.delta.data(), h.delta.size() * 2, cudaMemcpyHostToDevice, stream));
+    SW_CUDA(cudaMemcpyAsync(t_beg.p, h.inv_beg.data(), h.inv_beg.size() * 2, cudaMemcpyHostToDevice, stream));
+    SW_CUDA(cudaMemcpyAsync(t_src.p, h.inv_src.data(), h.inv_src.size() * 2, cudaMemcpyHostToDevice, stream));
+    SW_CUDA(cudaStreamSynchronize(stream));
+    tables.delta = t_delta.as<uint16_t>();
+    tables.inv_beg = t_beg.as<uint16_t>();
+    tables.inv_src = t_src.as<uint16_t>();
+    tables.n = (int)A.n;
+    tables.k = (int)A.k;
+  }
+
+  u32 read_u32(const u32* dptr) {
+    SW_CUDA(cudaMemcpyAsync(pinned.p, dptr, sizeof(u32), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaStreamSynchronize(stream));
+    return *pinned.as<u32>();
+  }
+
+  void count_launch(u64 c = 1) {
+    if (st) st->kernel_launches += c;
+  }
+
+  // Compact rows/vals by flags; returns kept count.
+  u32 compact(int W, const u64* rows, const u32* vals, const u32* flags, u32 m, u64* out_rows, u32* out_vals) {
+    pos.reserve(sizeof(u32) * (size_t)m);
+    scan_tmp.reserve(scan_temp_bytes(m));
+    u32* total = d_misc + 8;
+    launch_scan(flags, pos.as<u32>(), m, total, scan_tmp.p, stream);
+    launch_compact(W, rows, vals, flags, pos.as<u32>(), m, out_rows, out_vals, stream);
+    count_launch(4);
+    return read_u32(total);
+  }
+
+  void sort_rows(int R, u64* rows, u32* vals, u32 m) {
+    alt_rows.reserve(sizeof(u64) * R * (size_t)m);
+    alt_vals.reserve(sizeof(u32) * (size_t)m);
+    sort_tmp.reserve(sort_temp_bytes(R, m));
+    radix_sort_rows(R, rows, vals, alt_rows.as<u64>(), alt_vals.as<u32>(), m, sort_tmp.p, stream);
+    count_launch(3 * 8 * R);
+  }
+
+  void build_tree(int W, const u64* rows, u32 m, DevBuf& gamma, DevBuf& split) {
+    if (m < 2) return;
+    gamma.reserve(sizeof(u32) * m);
+    split.reserve(sizeof(u32) * m);
+    launch_trie_build(W, rows, m, gamma.as<u32>(), split.as<u32>(), stream);
+    count_launch();
+  }
+
+  void query(int W, int mode, const u64* S, u32 m, const DevBuf& gamma, const DevBuf& split, const u64* Q, u32 q,
+             int n, u32* flags, bool stop) {
+    if (!m || !q) return;
+    launch_trie_query(W, mode, S, m, m >= 2 ? gamma.as<u32>() : nullptr, m >= 2 ? split.as<u32>() : nullptr, Q, q,
+                      n, flags, d_misc, stop, stream);
+    count_launch();
+    if (st) {
+      st->trie_queries += q;
+      st->logical_pairs += (u64)m * q;
+    }
+  }
+
+  // One BFS layer on side X (forward = image, backward = preimage of complements).
+  void step(Side& X, bool forward, int W, int n, int k) {
+    const u32 m = X.count;
+    const u64 N = (u64)m * k;
+    if (N > 0xffffffffULL) throw std::runtime_error("layer exceeds 2^32 children");
+    const u32 Nc = (u32)N;
+    ch_rows.reserve(sizeof(u64) * W * N);
+    ch_vals.reserve(sizeof(u32) * N);
+    uq_rows.reserve(sizeof(u64) * W * N);
+    uq_vals.reserve(sizeof(u32) * N);
+    flags_a.reserve(sizeof(u32) * N);
+    flags_b.reserve(sizeof(u32) * N);
+    keep.reserve(sizeof(u32) * N);
+    launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream);
+    launch_iota(ch_vals.as<u32>(), Nc, stream);
+    count_launch(2);
+    if (st) st->subsets_expanded += N;
+    sort_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc);
+    launch_unique_flags(W, ch_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
+    count_launch();
+    const u32 u = compact(W, ch_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
+                          uq_vals.as<u32>());
+    // dominance: visited set inside the child, or a proper subset in the layer
+    launch_fill_u32(flags_a.as<u32>(), 0, u, stream);
+    launch_fill_u32(flags_b.as<u32>(), 0, u, stream);
+    count_launch(2);
+    if (X.vis_count)
+      query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split, uq_rows.as<u64>(), u, n,
+            flags_a.as<u32>(), false);
+    build_tree(W, uq_rows.as<u64>(), u, tmp_gamma, tmp_split);
+    query(W, kQueryProperSubset, uq_rows.as<u64>(), u, tmp_gamma, tmp_split, uq_rows.as<u64>(), u, n,
+          flags_b.as<u32>(), false);
+    launch_keep_flags(flags_a.as<u32>(), flags_b.as<u32>(), u, keep.as<u32>(), stream);
+    count_launch();
+    X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(u, 1));
+    new_vals.reserve(sizeof(u32) * (size_t)std::max<u32>(u, 1));
+    const u32 f = compact(W, uq_rows.as<u64>(), uq_vals.as<u32>(), keep.as<u32>(), u, X.rows_alt.as<u64>(),
+                          new_vals.as<u32>());
+    std::swap(X.rows.p, X.rows_alt.p);
+    std::swap(X.rows.cap, X.rows_alt.cap);
+    X.count = f;
+    if (st) st->subsets_kept += f;
+    auto L = std::make_unique<Layer>();
+    L->origin.reserve(sizeof(u32) * std::max<u32>(f, 1));
+    if (f)
+      SW_CUDA(cudaMemcpyAsync(L->origin.p, new_vals.p, sizeof(u32) * f, cudaMemcpyDeviceToDevice, stream));
+    L->count = f;
+    L->parent_count = m;
+    X.layers.push_back(std::move(L));
+    // visited := visited ∪ layer (both sorted, disjoint)
+    X.vis_alt.reserve(sizeof(u64) * W * ((size_t)X.vis_count + f + 1));
+    launch_merge(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
+    count_launch();
+    std::swap(X.vis.p, X.vis_alt.p);
+    std::swap(X.vis.cap, X.vis_alt.cap);
+    X.vis_count += f;
+    build_tree(W, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split);
+  }
+
+  // Trace letters of set `idx` at the top layer of side X down to depth 0.
+  std::vector<uint32_t> trace(const Side& X, u32 idx, u32* seed_index) {
+    std::vector<uint32_t> letters;  // from the top layer down
+    for (size_t d = X.layers.size(); d-- > 0;) {
+      const Layer& L = *X.layers[d];
+      u32 o = read_u32(L.origin.as<u32>() + idx);
+      letters.push_back(o / L.parent_count);
+      idx = o % L.parent_count;
+    }
+    if (seed_index) *seed_index = idx;
+    return letters;
+  }
+};
+
+Solver::Solver(int device) : device_(device), eng_(new Engine(device)) {}
+Solver::~Solver() = default;
+
+// ---------------------------------------------------------------------------
+// Exact::run (exact.cpp:37-97) on the device.
+// ---------------------------------------------------------------------------
+void Solver::exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw_stats& st) {
+  if (b.non_synchro || b.lower == b.upper) return;  // exact.cpp:45-47
+  if (A.n == 1) {                                   // exact.cpp:49-53
+    b.lower = b.upper = 0;
+    b.has_word = true;
+    b.word.clear();
+    return;
+  }
+  if (!is_synchronizing(A)) {
+    // The reference's Exact has no such check and runs until its bound; a
+    // non-synchronizing automaton is reported as such instead.
+    b.non_synchro = true;
+    return;
+  }
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  E.st = &st;
+  auto t0 = std::chrono::steady_clock::now();
+  const int n = (int)A.n, k = (int)A.k, W = words_for(n);
+  E.upload_tables(A);
+  E.F.reset();
+  E.B.reset();
+  // seeds
+  {
+    std::vector<u64> full(W, 0);
+    for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
+    E.F.rows.reserve(sizeof(u64) * W);
+    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
+    E.F.count = 1;
+    std::vector<uint32_t> seeds = backward_seeds(A);
+    std::vector<u64> rows((size_t)W * std::max<size_t>(seeds.size(), 1), 0);
+    for (size_t i = 0; i < seeds.size(); ++i) {
+      for (int q = 0; q < n; ++q)
+        if ((uint32_t)q != seeds[i]) rows[i * W + (q >> 6)] |= state_bit(q);  // complement of {seed}
+      E.B.seed_states.push_back(seeds[i]);
+    }
+    E.B.rows.reserve(sizeof(u64) * rows.size());
+    SW_CUDA(cudaMemcpyAsync(E.B.rows.p, rows.data(), sizeof(u64) * W * seeds.size(), cudaMemcpyHostToDevice,
+                            E.stream));
+    E.B.count = (u32)seeds.size();
+    // visited starts with the seeds (the reference's visited lists start empty;
+    // a seed can never be dominated by its own descendants' check either way)
+    E.F.vis.reserve(sizeof(u64) * W);
+    E.B.vis.reserve(sizeof(u64) * W * std::max<size_t>(seeds.size(), 1));
+    SW_CUDA(cudaMemcpyAsync(E.F.vis.p, E.F.rows.p, sizeof(u64) * W, cudaMemcpyDeviceToDevice, E.stream));
+    E.F.vis_count = 1;
+    if (!seeds.empty()) {
+      // seeds are already sorted ascending by state = descending by row value
+      // for complements; sort them properly via the row sort.
+      SW_CUDA(cudaMemcpyAsync(E.B.vis.p, E.B.rows.p, sizeof(u64) * W * seeds.size(), cudaMemcpyDeviceToDevice,
+                              E.stream));
+      E.keep.reserve(sizeof(u32) * seeds.size());
+      launch_iota(E.keep.as<u32>(), (u32)seeds.size(), E.stream);
+      E.sort_rows(W, E.B.vis.as<u64>(), E.keep.as<u32>(), (u32)seeds.size());
+      E.B.vis_count = (u32)seeds.size();
+      E.build_tree(W, E.B.vis.as<u64>(), E.B.vis_count, E.B.vis_gamma, E.B.vis_split);
+    }
+  }
+  const size_t budget = (size_t)cfg.max_memory_mb * 1024 * 1024;
+  const size_t row_bytes = sizeof(u64) * W;
+  const u64 max_rt = b.upper - 1;  // exact.cpp:65
+  u64 rt = 0;
+  bool found = false, oom = false;
+  u32 wit_q = 0, wit_s = 0;
+  while (rt < max_rt) {  // meet_in_the_middle.cpp:73
+    const bool fwd = E.F.count <= E.B.count;
+    Side& X = fwd ? E.F : E.B;
+    size_t live = (size_t)(E.F.count + E.F.vis_count + E.B.count + E.B.vis_count) * row_bytes;
+    size_t next = (size_t)X.count * k * (3 * row_bytes + 4 * sizeof(u32));
+    if (live + next > budget) {
+      oom = true;
+      break;
+    }
+    rt++;
+    E.step(X, fwd, W, n, k);
+    if (fwd) {
+      st.bfs_steps++;
+      E.build_tree(W, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split);
+    } else {
+      st.ibfs_steps++;
+    }
+    // meet check: some F disjoint from some B-complement (F ⊆ B)
+    SW_CUDA(cudaMemsetAsync(E.d_misc, 0, 4 * sizeof(u32), E.stream));
+    E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split, E.B.rows.as<u64>(), E.B.count,
+            n, nullptr, true);
+    st.meet_pairs += (u64)E.F.count * E.B.count;
+    SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    const u32* w = E.pinned.as<u32>();
+    if (w[0]) {
+      found = true;
+      wit_q = w[1];
+      wit_s = w[2];
+      break;
+    }
+    if (E.F.count == 0 || E.B.count == 0) break;  // a side died out: no reset word within reach
+  }
+  if (found) {
+    // word = forward letters (depth 1..df) then backward letters (depth db..1)
+    std::vector<uint32_t> fw = E.trace(E.F, wit_s, nullptr);
+    std::reverse(fw.begin(), fw.end());
+    u32 seed_idx = 0;
+    std::vector<uint32_t> bw = E.trace(E.B, wit_q, &seed_idx);
+    std::vector<uint32_t> word = fw;
+    word.insert(word.end(), bw.begin(), bw.end());
+    std::vector<uint32_t> img = apply_word(A, word);
+    if (img.size() != 1 || word.size() != rt)
+      throw std::runtime_error("internal error: reconstructed word does not synchronize (length " +
+                               std::to_string(word.size()) + ", image " + std::to_string(img.size()) + ")");
+    b.lower = std::max<u64>(b.lower, rt);
+    b.upper = rt;
+    b.has_word = true;
+    b.word = word;
+  } else {
+    // exact.cpp:148-164: every length <= rt is excluded; if that reaches the
+    // upper bound, the bound is the answer (its word, if any, came from the
+    // algorithm that set it).  Otherwise (memory budget) only a lower bound.
+    (void)oom;
+    rt++;
+    b.lower = std::max<u64>(b.lower, rt);
+    if (rt == b.upper) b.upper = rt;
+  }
+  st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  E.st = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Beam (beam.hpp:31-188): inverse BFS from the backward seeds keeping the
+// `beam_size` largest sets, ties by the reference's raw word order.
+// ---------------------------------------------------------------------------
+namespace {
+struct BeamRun {
+  u64 bound = 0;
+  bool has_word = false;
+  std::vector<uint32_t> word;
+};
+}  // namespace
+
+static BeamRun beam_cutoff(Engine& E, const Automaton& A, u32 beam_size, u64 max_mlsw, int64_t max_iter, sw_stats& st) {
+  const int n = (int)A.n, k = (int)A.k, W = words_for(n);
+  const int R = (n + 63) / 64 + 1;
+  BeamRun out;
+  out.bound = max_mlsw;
+  std::vector<uint32_t> seeds = backward_seeds(A);
+  Side& X = E.B;  // beam rows are plain (not complemented) preimages
+  X.reset();
+  std::vector<u64> rows((size_t)W * std::max<size_t>(seeds.size(), 1), 0);
+  for (size_t i = 0; i < seeds.size(); ++i) rows[i * W + (seeds[i] >> 6)] |= state_bit((int)seeds[i]);
+  X.rows.reserve(sizeof(u64) * rows.size());
+  SW_CUDA(cudaMemcpyAsync(X.rows.p, rows.data(), sizeof(u64) * W * seeds.size(), cudaMemcpyHostToDevice, E.stream));
+  X.count = (u32)seeds.size();
+  if (X.count == 0 || beam_size == 0) return out;
+  for (u64 len = 1; len < max_mlsw; ++len) {
+    if (max_iter >= 0 && (int64_t)len > max_iter) break;
+    const u32 m = X.count;
+    const u64 N = (u64)m * k;
+    if (N > 0xffffffffULL) throw std::runtime_error("beam layer exceeds 2^32 children");
+    const u32 Nc = (u32)N;
+    E.ch_rows.reserve(sizeof(u64) * W * N);
+    E.keys.reserve(sizeof(u64) * R * N);
+    E.ch_vals.reserve(sizeof(u32) * N);
+    E.flags_a.reserve(sizeof(u32) * N);
+    E.uq_vals.reserve(sizeof(u32) * N);
+    E.keys_alt.reserve(sizeof(u64) * R * N);
+    launch_expand(W, false, X.rows.as<u64>(), m, E.tables, E.ch_rows.as<u64>(), E.stream);
+    launch_beam_keys(W, E.ch_rows.as<u64>(), Nc, n, R, E.keys.as<u64>(), E.stream);
+    launch_iota(E.ch_vals.as<u32>(), Nc, E.stream);
+    E.count_launch(3);
+    st.subsets_expanded += N;
+    E.sort_rows(R, E.keys.as<u64>(), E.ch_vals.as<u32>(), Nc);
+    // beam.hpp:173-177: the largest set is first; Q means done
+    SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.keys.p, sizeof(u64), cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    if (*E.pinned.as<u64>() == 0) {
+      u32 first_val = 0;
+      SW_CUDA(cudaMemcpy(&first_val, E.ch_vals.p, sizeof(u32), cudaMemcpyDeviceToHost));
+      // word: letters from this layer down to the first, applied in that order
+      std::vector<uint32_t> letters;
+      letters.push_back(first_val / m);
+      u32 idx = first_val % m;
+      for (size_t d = X.layers.size(); d-- > 0;) {
+        const Layer& L = *X.layers[d];
+        u32 o = E.read_u32(L.origin.as<u32>() + idx);
+        letters.push_back(o / L.parent_count);
+        idx = o % L.parent_count;
+      }
+      out.bound = len;
+      out.word = letters;
+      std::vector<uint32_t> img = apply_word(A, out.word);
+      out.has_word = img.size() == 1 && out.word.size() == len;
+      return out;
+    }
+    // keep_unique + truncate (beam.hpp:179-182)
+    launch_unique_flags(R, E.keys.as<u64>(), Nc, E.flags_a.as<u32>(), E.stream);
+    E.count_launch();
+    E.uq_rows.reserve(sizeof(u64) * R * N);
+    u32 u = E.compact(R, E.keys.as<u64>(), E.ch_vals.as<u32>(), E.flags_a.as<u32>(), Nc, E.uq_rows.as<u64>(),
+                      E.uq_vals.as<u32>());
+    u32 keep = std::min<u32>(u, beam_size);
+    X.rows_alt.reserve(sizeof(u64) * W * std::max<u32>(keep, 1));
+    launch_gather_rows(W, E.ch_rows.as<u64>(), E.uq_vals.as<u32>(), keep, X.rows_alt.as<u64>(), E.stream);
+    E.count_launch();
+    std::swap(X.rows.p, X.rows_alt.p);
+    std::swap(X.rows.cap, X.rows_alt.cap);
+    auto L = std::make_unique<Layer>();
+    L->origin.reserve(sizeof(u32) * std::max<u32>(keep, 1));
+    SW_CUDA(cudaMemcpyAsync(L->origin.p, E.uq_vals.p, sizeof(u32) * keep, cudaMemcpyDeviceToDevice, E.stream));
+    L->count = keep;
+    L->parent_count = m;
+    X.layers.push_back(std::move(L));
+    X.count = keep;
+  }
+  return out;
+}
+
+void Solver::beam(const Automaton& A0, const sw_beam_config& cfg, Bounds& b, sw_stats& st) {
+  if (b.non_synchro || b.lower == b.upper) return;  // beam.hpp:34-40
+  if (A0.n == 1) {                                  // beam.hpp:42-46
+    b.lower = b.upper = 0;
+    b.has_word = true;
+    b.word.clear();
+    return;
+  }
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  E.st = &st;
+  auto t0 = std::chrono::steady_clock::now();
+  // presort (beam.hpp:54-63, 351-369): states ordered by in-degree ascending
+  std::vector<uint32_t> perm(A0.n);
+  std::iota(perm.begin(), perm.end(), 0u);
+  if (cfg.presort_indeg) {
+    std::vector<std::pair<double, int>> d(A0.n);
+    for (uint32_t q = 0; q < A0.n; ++q) d[q] = {0.0, (int)q};
+    for (uint32_t q = 0; q < A0.n; ++q)
+      for (uint32_t a = 0; a < A0.k; ++a) d[A0.at(q, a)].first++;
+    std::sort(d.begin(), d.end());
+    for (uint32_t q = 0; q < A0.n; ++q) perm[d[q].second] = q;
+  }
+  Automaton A = permute(A0, perm);
+  E.upload_tables(A);
+  BeamRun run;
+  if (cfg.dynamic) {  // beam.hpp:66-86
+    using cost_t = long double;
+    const uint32_t minb = (uint32_t)cfg.min_beam_size, maxb = (uint32_t)cfg.max_beam_size;
+    run = beam_cutoff(E, A, minb, b.upper, cfg.max_iter, st);
+    uint32_t bound = (uint32_t)run.bound;
+    cost_t exact_cost = 2 * std::pow(static_cast<cost_t>(A.k), (bound + 1) / 2);
+    cost_t proposed = std::round(exact_cost * (cost_t)cfg.beam_exact_ratio / bound);
+    uint32_t bs = (uint32_t)std::clamp<cost_t>(proposed, (cost_t)minb, (cost_t)maxb);
+    if (bs > minb) {
+      // the second run searches below the first bound; it returns that bound
+      // unchanged (and no word) when it finds nothing shorter
+      BeamRun second = beam_cutoff(E, A, bs, bound, cfg.max_iter, st);
+      if (second.bound < bound) run = second;
+    }
+  } else {
+    run = beam_cutoff(E, A, (uint32_t)cfg.beam_size, b.upper, cfg.max_iter, st);
+  }
+  const uint32_t bound = (uint32_t)run.bound;  // the reference stores the bound in a uint
+  b.upper = bound;
+  if (run.has_word && run.word.size() == bound) {
+    b.has_word = true;
+    b.word = run.word;
+  } else if (b.has_word && b.word.size() != b.upper) {
+    b.has_word = false;
+  }
+  st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  E.st = nullptr;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel-level helpers.
+// ---------------------------------------------------------------------------
+void Solver::apply_transition(const Automaton& A, uint32_t letter, bool inverse, const uint64_t* from, uint64_t* to,
+                              uint64_t count) {
+  if (letter >= A.k) throw std::invalid_argument("letter out of range");
+  if (count == 0) return;
+  if (count > 0xffffffffULL) throw std::invalid_argument("count exceeds 2^32");
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  const int n = (int)A.n, W = words_for(n);
+  // single-letter automaton view so the kernel writes one block
+  Automaton one;
+  one.n = A.n;
+  one.k = 1;
+  one.t.resize(A.n);
+  for (uint32_t q = 0; q < A.n; ++q) one.t[q] = A.at(q, letter);
+  E.upload_tables(one);
+  std::vector<u64> rows((size_t)W * count);
+  to_device_rows(from, count, A.n, W, rows.data());
+  E.uq_rows.reserve(sizeof(u64) * rows.size());
+  E.ch_rows.reserve(sizeof(u64) * rows.size());
+  SW_CUDA(cudaMemcpyAsync(E.uq_rows.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+  launch_expand(W, !inverse, E.uq_rows.as<u64>(), (u32)count, E.tables, E.ch_rows.as<u64>(), E.stream);
+  SW_CUDA(cudaMemcpyAsync(rows.data(), E.ch_rows.p, sizeof(u64) * rows.size(), cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  from_device_rows(rows.data(), count, A.n, W, to);
+}
+
+void Solver::subsets_check(uint32_t n, const uint64_t* sets, uint64_t set_count, const uint64_t* checks,
+                           uint64_t check_count, bool proper, uint8_t* results) {
+  if (n == 0 || n > (uint32_t)kMaxStates) throw std::invalid_argument("n out of range");
+  if (set_count > 0xffffffffULL || check_count > 0xffffffffULL) throw std::invalid_argument("count exceeds 2^32");
+  std::fill(results, results + check_count, 0);
+  if (!set_count || !check_count) return;
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  const int W = words_for((int)n);
+  std::vector<u64> srows((size_t)W * set_count), qrows((size_t)W * check_count);
+  to_device_rows(sets, set_count, n, W, srows.data());
+  to_device_rows(checks, check_count, n, W, qrows.data());
+  const u32 m = (u32)set_count, q = (u32)check_count;
+  E.uq_rows.reserve(sizeof(u64) * srows.size());
+  E.uq_vals.reserve(sizeof(u32) * m);
+  E.ch_rows.reserve(sizeof(u64) * qrows.size());
+  E.flags_a.reserve(sizeof(u32) * m);
+  E.flags_b.reserve(sizeof(u32) * q);
+  E.keys.reserve(sizeof(u64) * srows.size());
+  SW_CUDA(cudaMemcpyAsync(E.uq_rows.p, srows.data(), sizeof(u64) * srows.size(), cudaMemcpyHostToDevice, E.stream));
+  SW_CUDA(cudaMemcpyAsync(E.ch_rows.p, qrows.data(), sizeof(u64) * qrows.size(), cudaMemcpyHostToDevice, E.stream));
+  // sort + unique the set list (check_contains_subset sorts both, :30-33)
+  launch_iota(E.uq_vals.as<u32>(), m, E.stream);
+  E.sort_rows(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), m);
+  launch_unique_flags(W, E.uq_rows.as<u64>(), m, E.flags_a.as<u32>(), E.stream);
+  u32 u = E.compact(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), E.flags_a.as<u32>(), m, E.keys.as<u64>(), nullptr);
+  E.build_tree(W, E.keys.as<u64>(), u, E.tmp_gamma, E.tmp_split);
+  launch_fill_u32(E.flags_b.as<u32>(), 0, q, E.stream);
+  E.query(W, proper ? kQueryProperSubset : kQuerySubset, E.keys.as<u64>(), u, E.tmp_gamma, E.tmp_split,
+          E.ch_rows.as<u64>(), q, (int)n, E.flags_b.as<u32>(), false);
+  std::vector<u32> flags(q);
+  SW_CUDA(cudaMemcpyAsync(flags.data(), E.flags_b.p, sizeof(u32) * q, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  for (u32 i = 0; i < q; ++i) results[i] = flags[i] ? 1 : 0;
+}
+
+uint64_t Solver::sort_unique(uint32_t n, uint64_t* sets, uint64_t count) {
+  if (n == 0 || n > (uint32_t)kMaxStates) throw std::invalid_argument("n out of range");
+  if (count > 0xffffffffULL) throw std::invalid_argument("count exceeds 2^32");
+  if (count == 0) return 0;
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  const int W = words_for((int)n);
+  std::vector<u64> rows((size_t)W * count);
+  to_device_rows(sets, count, n, W, rows.data());
+  const u32 m = (u32)count;
+  E.uq_rows.reserve(sizeof(u64) * rows.size());
+  E.uq_vals.reserve(sizeof(u32) * m);
+  E.keys.reserve(sizeof(u64) * rows.size());
+  E.flags_a.reserve(sizeof(u32) * m);
+  SW_CUDA(cudaMemcpyAsync(E.uq_rows.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+  launch_iota(E.uq_vals.as<u32>(), m, E.stream);
+  E.sort_rows(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), m);
+  launch_unique_flags(W, E.uq_rows.as<u64>(), m, E.flags_a.as<u32>(), E.stream);
+  u32 u = E.compact(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), E.flags_a.as<u32>(), m, E.keys.as<u64>(), nullptr);
+  SW_CUDA(cudaMemcpyAsync(rows.data(), E.keys.p, sizeof(u64) * W * u, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  from_device_rows(rows.data(), u, n, W, sets);
+  return u;
+}
+
+}  // namespace sw

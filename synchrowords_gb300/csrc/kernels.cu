@@ -1,0 +1,924 @@
+// Device kernels of the exact search: warp-per-subset layer expansion, radix
+// sort / unique, stream compaction, the binary radix tree over a sorted layer
+// and the tree-walking subset queries.  All integer bitset work; see
+// common.cuh for the row layout and kernels.cuh for the reference functions
+// each kernel replaces.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "kernels.cuh"
+
+namespace sw {
+
+namespace {
+
+constexpr u32 kFull = 0xffffffffu;
+
+__device__ __forceinline__ u32 lanemask_lt() {
+  u32 m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+int sm_count() {
+  static int cached = 0;
+  if (!cached) {
+    int dev = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    SW_CUDA(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev));
+  }
+  return cached;
+}
+
+template <int W>
+__device__ __forceinline__ bool row_less(const u64* a, const u64* b) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    u64 x = a[w], y = b[w];
+    if (x != y) return x < y;
+  }
+  return false;
+}
+
+template <int W>
+__device__ __forceinline__ bool row_eq(const u64* a, const u64* b) {
+#pragma unroll
+  for (int w = 0; w < W; ++w)
+    if (a[w] != b[w]) return false;
+  return true;
+}
+
+}  // namespace
+
+// ===========================================================================
+// Layer expansion.  One warp per input set.  The set row is staged in shared
+// memory; lane l decides output states l, l+32, ... by a gather:
+//   preimage  out[p] = S[delta_a(p)]                  (delta in smem)
+//   image     out[t] = OR_{q : delta_a(q) = t} S[q]   (preimage CSR in smem)
+// and each 32-state round becomes half an output word through __ballot_sync
+// (bit-reversed into the MSB-first layout).  Both directions are
+// gathers, so no atomics are needed.
+// ===========================================================================
+template <int W, bool kImage>
+__global__ void __launch_bounds__(256) k_expand(const u64* __restrict__ in, u32 m, TransTables t,
+                                                u64* __restrict__ out) {
+  extern __shared__ uint16_t s_tab[];
+  __shared__ u64 s_row[8][W];
+  const int n = t.n, k = t.k;
+  uint16_t* s_a = s_tab;                  // delta (preimage) or inv_beg (image)
+  uint16_t* s_b = s_tab + k * (n + 1);    // inv_src (image)
+  if (kImage) {
+    for (int i = threadIdx.x; i < k * (n + 1); i += blockDim.x) s_a[i] = t.inv_beg[i];
+    for (int i = threadIdx.x; i < k * n; i += blockDim.x) s_b[i] = t.inv_src[i];
+  } else {
+    for (int i = threadIdx.x; i < k * n; i += blockDim.x) s_a[i] = t.delta[i];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32 stride = gridDim.x * 8u;
+  const int rounds = (n + 31) >> 5;
+  for (u32 i = blockIdx.x * 8u + warp; i < m; i += stride) {
+    if (lane < W) s_row[warp][lane] = in[(size_t)i * W + lane];
+    __syncwarp();
+    for (int a = 0; a < k; ++a) {
+      u64 word = 0;
+      for (int r = 0; r < rounds; ++r) {
+        const int q = r * 32 + lane;
+        bool bit = false;
+        if (q < n) {
+          if (kImage) {
+            const int b = s_a[a * (n + 1) + q], e = s_a[a * (n + 1) + q + 1];
+            for (int j = b; j < e; ++j) {
+              const int p = s_b[a * n + j];
+              if ((s_row[warp][p >> 6] >> (63 - (p & 63))) & 1ULL) {
+                bit = true;
+                break;
+              }
+            }
+          } else {
+            const int p = s_a[a * n + q];
+            bit = (s_row[warp][p >> 6] >> (63 - (p & 63))) & 1ULL;
+          }
+        }
+        const u32 bal = __ballot_sync(kFull, bit);
+        if (lane == (r >> 1)) {
+          const u64 v = (u64)__brev(bal);
+          word |= (r & 1) ? v : (v << 32);
+        }
+      }
+      if (lane < W) out[((size_t)a * m + i) * W + lane] = word;
+    }
+    __syncwarp();
+  }
+}
+
+void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s) {
+  if (m == 0) return;
+  size_t smem = image ? sizeof(uint16_t) * (size_t)t.k * (2 * t.n + 1) : sizeof(uint16_t) * (size_t)t.k * t.n;
+  u32 blocks = std::min<u32>((m + 7) / 8, (u32)sm_count() * 8);
+#define SW_EXP(WW)                                                                                  \
+  case WW:                                                                                          \
+    if (image) {                                                                                    \
+      if (smem > 48 * 1024)                                                                         \
+        SW_CUDA(cudaFuncSetAttribute(k_expand<WW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                   \
+      k_expand<WW, true><<<blocks, 256, smem, s>>>(in, m, t, out);                                  \
+    } else {                                                                                        \
+      if (smem > 48 * 1024)                                                                         \
+        SW_CUDA(cudaFuncSetAttribute(k_expand<WW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                     (int)smem));                                                   \
+      k_expand<WW, false><<<blocks, 256, smem, s>>>(in, m, t, out);                                 \
+    }                                                                                               \
+    break;
+  switch (W) {
+    SW_EXP(1)
+    SW_EXP(2)
+    SW_EXP(4)
+    SW_EXP(8)
+    default:
+      throw std::runtime_error("expand: unsupported width");
+  }
+#undef SW_EXP
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Device-wide exclusive scan of u32 (three kernels: tile sums, scan of the
+// tile sums in one block, tile scans with carry-in).
+// ===========================================================================
+namespace {
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr u32 kScanTile = kScanThreads * kScanItems;
+
+// Exclusive scan across a 1024-thread block; returns the block total.
+__device__ u32 block_exclusive_scan(u32 v, u32& total) {
+  __shared__ u32 s_warp[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    u32 y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    u32 w = (lane < (int)(blockDim.x >> 5)) ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      u32 y = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += y;
+    }
+    s_warp[lane] = w;
+  }
+  __syncthreads();
+  total = s_warp[(blockDim.x >> 5) - 1];
+  u32 excl = x - v + (warp ? s_warp[warp - 1] : 0);
+  __syncthreads();
+  return excl;
+}
+}  // namespace
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const u32* __restrict__ in, u32 n, u32* partial) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  u32 s = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j)
+    if (base + j < n) s += in[base + j];
+  u32 tot;
+  block_exclusive_scan(s, tot);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(u32* partial, u32 nb, u32* total_dev) {
+  u32 carry = 0;
+  for (u32 base = 0; base < nb; base += kScanTile) {
+    u32 v[kScanItems];
+    u32 s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      u32 idx = base + threadIdx.x * kScanItems + j;
+      v[j] = idx < nb ? partial[idx] : 0;
+      s += v[j];
+    }
+    u32 tot;
+    u32 ex = block_exclusive_scan(s, tot);
+    u32 run = carry + ex;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      u32 idx = base + threadIdx.x * kScanItems + j;
+      if (idx < nb) partial[idx] = run;
+      run += v[j];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && total_dev) *total_dev = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(const u32* __restrict__ in, u32* __restrict__ out, u32 n,
+                                                             const u32* partial) {
+  const size_t base = (size_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  u32 v[kScanItems];
+  u32 s = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    v[j] = (base + j < n) ? in[base + j] : 0;
+    s += v[j];
+  }
+  u32 tot;
+  u32 run = block_exclusive_scan(s, tot) + partial[blockIdx.x];
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j) {
+    if (base + j < n) out[base + j] = run;
+    run += v[j];
+  }
+}
+
+size_t scan_temp_bytes(u32 n) { return sizeof(u32) * ((n + kScanTile - 1) / kScanTile + 1); }
+
+void launch_scan(const u32* in, u32* out, u32 n, u32* total_dev, void* temp, cudaStream_t s) {
+  if (n == 0) {
+    if (total_dev) SW_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(u32), s));
+    return;
+  }
+  u32 nb = (n + kScanTile - 1) / kScanTile;
+  u32* partial = static_cast<u32*>(temp);
+  k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, n, partial);
+  k_scan_partials<<<1, kScanThreads, 0, s>>>(partial, nb, total_dev);
+  k_scan_final<<<nb, kScanThreads, 0, s>>>(in, out, n, partial);
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Radix sort of rows (R words, word 0 most significant) with u32 payload.
+// Stable LSD over 8-bit digits; digits that are constant over all rows are
+// skipped (their OR == AND).  Large inputs: per-pass upsweep (tile digit
+// counts) -> scan -> downsweep (stable in-tile rank via __match_any_sync,
+// scatter of whole rows).  Inputs of at most one shared-memory tile are sorted
+// by a single block in shared memory.
+// ===========================================================================
+namespace {
+constexpr int kRsThreads = 256;
+constexpr int kRsRounds = 8;
+constexpr u32 kRsTile = kRsThreads * kRsRounds;
+
+template <int R>
+constexpr u32 small_sort_max() {
+  return R <= 4 ? 2048u : 1024u;
+}
+
+// Per-round stable ranking inside a 256-thread block.  `d` is this thread's
+// digit (256 = no item).  s_base[256] carries counts of earlier rounds,
+// s_wcnt[8][256] is scratch.  Returns the item's rank among equal digits in
+// the block so far.
+__device__ __forceinline__ u32 block_round_rank(u32 d, u32* s_base, u32 (*s_wcnt)[256]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32 peers = __match_any_sync(kFull, d);
+  const u32 lrank = __popc(peers & lanemask_lt());
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s_wcnt[warp][lane * 8 + j] = 0;
+  __syncwarp();
+  if (d < 256 && lrank == 0) s_wcnt[warp][d] = __popc(peers);
+  __syncthreads();
+  {
+    const int t = threadIdx.x;  // digit owned by this thread
+    u32 run = s_base[t];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      u32 c = s_wcnt[w][t];
+      s_wcnt[w][t] = run;
+      run += c;
+    }
+    s_base[t] = run;
+  }
+  __syncthreads();
+  u32 r = (d < 256) ? s_wcnt[warp][d] + lrank : 0;
+  __syncthreads();
+  return r;
+}
+}  // namespace
+
+template <int R>
+__global__ void k_or_and(const u64* __restrict__ rows, u32 m, u64* orv, u64* andv) {
+  u64 o[R], a[R];
+#pragma unroll
+  for (int w = 0; w < R; ++w) {
+    o[w] = 0;
+    a[w] = ~0ULL;
+  }
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int w = 0; w < R; ++w) {
+      u64 v = rows[(size_t)i * R + w];
+      o[w] |= v;
+      a[w] &= v;
+    }
+  }
+#pragma unroll
+  for (int w = 0; w < R; ++w) {
+    u64 x = o[w], y = a[w];
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      x |= __shfl_xor_sync(kFull, x, off);
+      y &= __shfl_xor_sync(kFull, y, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicOr(orv + w, x);
+      atomicAnd(andv + w, y);
+    }
+  }
+}
+
+template <int R>
+__global__ void __launch_bounds__(kRsThreads) k_rs_upsweep(const u64* __restrict__ keys, u32 m, int word, int shift,
+                                                           u32 ntiles, u32* counts) {
+  __shared__ u32 hist[256];
+  hist[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRsTile;
+  for (int r = 0; r < kRsRounds; ++r) {
+    size_t idx = base + r * kRsThreads + threadIdx.x;
+    u32 d = 256;
+    if (idx < m) d = (u32)((keys[idx * R + word] >> shift) & 255ULL);
+    u32 peers = __match_any_sync(kFull, d);
+    if (d < 256 && __popc(peers & lanemask_lt()) == 0) atomicAdd(&hist[d], __popc(peers));
+  }
+  __syncthreads();
+  counts[threadIdx.x * ntiles + blockIdx.x] = hist[threadIdx.x];
+}
+
+template <int R>
+__global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(const u64* __restrict__ keys, const u32* __restrict__ vals,
+                                                             u32 m, int word, int shift, u32 ntiles,
+                                                             const u32* __restrict__ offsets, u64* __restrict__ keys_out,
+                                                             u32* __restrict__ vals_out) {
+  __shared__ u32 s_off[256];
+  __shared__ u32 s_base[256];
+  __shared__ u32 s_wcnt[8][256];
+  s_off[threadIdx.x] = offsets[threadIdx.x * ntiles + blockIdx.x];
+  s_base[threadIdx.x] = 0;
+  __syncthreads();
+  const size_t base = (size_t)blockIdx.x * kRsTile;
+  for (int r = 0; r < kRsRounds; ++r) {
+    size_t idx = base + r * kRsThreads + threadIdx.x;
+    const bool valid = idx < m;
+    u64 row[R];
+    u32 val = 0;
+    u32 d = 256;
+    if (valid) {
+#pragma unroll
+      for (int w = 0; w < R; ++w) row[w] = keys[idx * R + w];
+      val = vals[idx];
+      u64 kw = 0;
+#pragma unroll
+      for (int w = 0; w < R; ++w)
+        if (w == word) kw = row[w];
+      d = (u32)((kw >> shift) & 255ULL);
+    }
+    u32 rank = block_round_rank(d, s_base, s_wcnt);
+    if (valid) {
+      size_t dst = (size_t)s_off[d] + rank;
+#pragma unroll
+      for (int w = 0; w < R; ++w) keys_out[dst * R + w] = row[w];
+      vals_out[dst] = val;
+    }
+  }
+}
+
+// Whole sort in one block, rows in shared memory (m <= small_sort_max<R>()).
+template <int R>
+__global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u32 m) {
+  extern __shared__ u64 s_mem[];
+  u64* ka = s_mem;
+  u64* kb = ka + (size_t)m * R;
+  u32* va = reinterpret_cast<u32*>(kb + (size_t)m * R);
+  u32* vb = va + m;
+  __shared__ u32 s_hist[256];
+  __shared__ u32 s_base[256];
+  __shared__ u32 s_wcnt[8][256];
+  __shared__ u64 s_or[R], s_and[R];
+  if (threadIdx.x < R) {
+    s_or[threadIdx.x] = 0;
+    s_and[threadIdx.x] = ~0ULL;
+  }
+  __syncthreads();
+  {
+    u64 o[R], a[R];
+#pragma unroll
+    for (int w = 0; w < R; ++w) {
+      o[w] = 0;
+      a[w] = ~0ULL;
+    }
+    for (u32 i = threadIdx.x; i < m; i += kRsThreads) {
+#pragma unroll
+      for (int w = 0; w < R; ++w) {
+        u64 v = keys[(size_t)i * R + w];
+        ka[(size_t)i * R + w] = v;
+        o[w] |= v;
+        a[w] &= v;
+      }
+      va[i] = vals[i];
+    }
+#pragma unroll
+    for (int w = 0; w < R; ++w) {
+      atomicOr(&s_or[w], o[w]);
+      atomicAnd(&s_and[w], a[w]);
+    }
+  }
+  __syncthreads();
+  const u32 rounds = (m + kRsThreads - 1) / kRsThreads;
+  for (int word = R - 1; word >= 0; --word) {
+    const u64 vary = s_or[word] ^ s_and[word];
+    for (int shift = 0; shift < 64; shift += 8) {
+      if (((vary >> shift) & 255ULL) == 0) continue;
+      s_hist[threadIdx.x] = 0;
+      s_base[threadIdx.x] = 0;
+      __syncthreads();
+      for (u32 i = threadIdx.x; i < m; i += kRsThreads)
+        atomicAdd(&s_hist[(ka[(size_t)i * R + word] >> shift) & 255ULL], 1u);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        u32 run = 0;
+        for (int d = 0; d < 256; ++d) {
+          u32 c = s_hist[d];
+          s_hist[d] = run;
+          run += c;
+        }
+      }
+      __syncthreads();
+      for (u32 r = 0; r < rounds; ++r) {
+        u32 i = r * kRsThreads + threadIdx.x;
+        u32 d = i < m ? (u32)((ka[(size_t)i * R + word] >> shift) & 255ULL) : 256u;
+        u32 rank = block_round_rank(d, s_base, s_wcnt);
+        if (d < 256) {
+          u32 dst = s_hist[d] + rank;
+#pragma unroll
+          for (int w = 0; w < R; ++w) kb[(size_t)dst * R + w] = ka[(size_t)i * R + w];
+          vb[dst] = va[i];
+        }
+      }
+      __syncthreads();
+      u64* tk = ka;
+      ka = kb;
+      kb = tk;
+      u32* tv = va;
+      va = vb;
+      vb = tv;
+    }
+  }
+  for (u32 i = threadIdx.x; i < m; i += kRsThreads) {
+#pragma unroll
+    for (int w = 0; w < R; ++w) keys[(size_t)i * R + w] = ka[(size_t)i * R + w];
+    vals[i] = va[i];
+  }
+}
+
+size_t sort_temp_bytes(int R, u32 m) {
+  u32 ntiles = (m + kRsTile - 1) / kRsTile;
+  size_t counts = sizeof(u32) * 256 * (size_t)ntiles;
+  // counts + offsets + scan partials + or/and words (+ host-visible copy)
+  return 2 * counts + scan_temp_bytes(256 * ntiles) + 2 * sizeof(u64) * 16 + 256;
+}
+
+template <int R>
+static void radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+  if (m <= 1) return;
+  if (m <= small_sort_max<R>()) {
+    size_t smem = (size_t)m * (2 * R * sizeof(u64) + 2 * sizeof(u32));
+    SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m);
+    SW_LAUNCH_CHECK();
+    return;
+  }
+  const u32 ntiles = (m + kRsTile - 1) / kRsTile;
+  char* t = static_cast<char*>(temp);
+  u32* counts = reinterpret_cast<u32*>(t);
+  u32* offsets = counts + 256 * (size_t)ntiles;
+  u64* orv = reinterpret_cast<u64*>(offsets + 256 * (size_t)ntiles);
+  u64* andv = orv + 16;
+  void* scan_tmp = andv + 16;
+  SW_CUDA(cudaMemsetAsync(orv, 0, sizeof(u64) * R, s));
+  SW_CUDA(cudaMemsetAsync(andv, 0xff, sizeof(u64) * R, s));
+  u32 blocks = std::min<u32>((m + 255) / 256, (u32)sm_count() * 4);
+  k_or_and<R><<<blocks, 256, 0, s>>>(keys, m, orv, andv);
+  SW_LAUNCH_CHECK();
+  u64 h_or[R], h_and[R];
+  SW_CUDA(cudaMemcpyAsync(h_or, orv, sizeof(u64) * R, cudaMemcpyDeviceToHost, s));
+  SW_CUDA(cudaMemcpyAsync(h_and, andv, sizeof(u64) * R, cudaMemcpyDeviceToHost, s));
+  SW_CUDA(cudaStreamSynchronize(s));
+  u64 *ki = keys, *ko = keys_alt;
+  u32 *vi = vals, *vo = vals_alt;
+  for (int word = R - 1; word >= 0; --word) {
+    const u64 vary = h_or[word] ^ h_and[word];
+    for (int shift = 0; shift < 64; shift += 8) {
+      if (((vary >> shift) & 255ULL) == 0) continue;
+      k_rs_upsweep<R><<<ntiles, kRsThreads, 0, s>>>(ki, m, word, shift, ntiles, counts);
+      launch_scan(counts, offsets, 256 * ntiles, nullptr, scan_tmp, s);
+      k_rs_downsweep<R><<<ntiles, kRsThreads, 0, s>>>(ki, vi, m, word, shift, ntiles, offsets, ko, vo);
+      SW_LAUNCH_CHECK();
+      std::swap(ki, ko);
+      std::swap(vi, vo);
+    }
+  }
+  if (ki != keys) {
+    SW_CUDA(cudaMemcpyAsync(keys, ki, sizeof(u64) * R * (size_t)m, cudaMemcpyDeviceToDevice, s));
+    SW_CUDA(cudaMemcpyAsync(vals, vi, sizeof(u32) * (size_t)m, cudaMemcpyDeviceToDevice, s));
+  }
+}
+
+void radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+  switch (R) {
+    case 1: return radix_sort_rows_t<1>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 2: return radix_sort_rows_t<2>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 3: return radix_sort_rows_t<3>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 4: return radix_sort_rows_t<4>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 5: return radix_sort_rows_t<5>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 6: return radix_sort_rows_t<6>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 7: return radix_sort_rows_t<7>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 8: return radix_sort_rows_t<8>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 9: return radix_sort_rows_t<9>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    default: throw std::runtime_error("radix_sort_rows: unsupported row width");
+  }
+}
+
+// ===========================================================================
+// Unique flags, compaction and small helpers.
+// ===========================================================================
+template <int W>
+__global__ void k_unique_flags(const u64* __restrict__ rows, u32 m, u32* flags) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  flags[i] = (i == 0) ? 1u : (row_eq<W>(rows + (size_t)i * W, rows + (size_t)(i - 1) * W) ? 0u : 1u);
+}
+
+template <int W>
+__global__ void k_compact(const u64* __restrict__ rows, const u32* __restrict__ vals, const u32* __restrict__ flags,
+                          const u32* __restrict__ pos, u32 m, u64* __restrict__ out_rows, u32* __restrict__ out_vals) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m || !flags[i]) return;
+  const u32 d = pos[i];
+#pragma unroll
+  for (int w = 0; w < W; ++w) out_rows[(size_t)d * W + w] = rows[(size_t)i * W + w];
+  if (out_vals) out_vals[d] = vals[i];
+}
+
+template <int W>
+__global__ void k_complement(u64* rows, u32 m, int n) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+#pragma unroll
+  for (int w = 0; w < W; ++w) rows[(size_t)i * W + w] = ~rows[(size_t)i * W + w] & valid_mask(n, w);
+}
+
+template <int W>
+__global__ void k_popcount(const u64* rows, u32 m, u32* out) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  u32 c = 0;
+#pragma unroll
+  for (int w = 0; w < W; ++w) c += __popcll(rows[(size_t)i * W + w]);
+  out[i] = c;
+}
+
+__global__ void k_keep_flags(const u32* a, const u32* b, u32 m, u32* out) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  out[i] = (a[i] == 0 && b[i] == 0) ? 1u : 0u;
+}
+
+__global__ void k_fill_u32(u32* p, u32 v, u32 m) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) p[i] = v;
+}
+
+#define SW_DISPATCH_W(W, ...)                               \
+  switch (W) {                                              \
+    case 1: { constexpr int WW = 1; __VA_ARGS__; } break;   \
+    case 2: { constexpr int WW = 2; __VA_ARGS__; } break;   \
+    case 4: { constexpr int WW = 4; __VA_ARGS__; } break;   \
+    case 8: { constexpr int WW = 8; __VA_ARGS__; } break;   \
+    default: throw std::runtime_error("unsupported set width"); \
+  }
+
+void launch_unique_flags(int W, const u64* rows, u32 m, u32* flags, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_unique_flags<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, flags)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_compact(int W, const u64* rows, const u32* vals, const u32* flags, const u32* pos, u32 m, u64* out_rows,
+                    u32* out_vals, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_compact<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, vals, flags, pos, m, out_rows, out_vals)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_complement(int W, u64* rows, u32 m, int n, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_complement<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, n)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_popcount(int W, const u64* rows, u32 m, u32* out, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_popcount<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, out)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t s) {
+  if (!m) return;
+  k_keep_flags<<<(m + 255) / 256, 256, 0, s>>>(a, b, m, out);
+  SW_LAUNCH_CHECK();
+}
+
+void launch_fill_u32(u32* p, u32 value, u32 m, cudaStream_t s) {
+  if (!m) return;
+  k_fill_u32<<<(m + 255) / 256, 256, 0, s>>>(p, value, m);
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Binary radix tree over sorted unique rows (Karras, "Maximizing parallelism
+// in the construction of BVHs, octrees, and k-d trees", HPG 2012).  Internal
+// node i covers [min(i,j), max(i,j)]; its keys share their first split[i]
+// bits; the left child [lo, gamma] has 0 at bit split[i], the right child
+// [gamma+1, hi] has 1.  This is the explicit form of the reference's implicit
+// trie recursion over bit depth (subsets_implicit_trie.hpp:224-265), with
+// constant-bit levels collapsed.
+// ===========================================================================
+template <int W>
+__device__ __forceinline__ int row_lcp(const u64* a, const u64* b) {
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    u64 x = a[w] ^ b[w];
+    if (x) return w * 64 + __clzll(x);
+  }
+  return W * 64;
+}
+
+template <int W>
+__global__ void k_trie_build(const u64* __restrict__ rows, u32 m, u32* __restrict__ gamma, u32* __restrict__ split) {
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long)m - 1) return;
+  const u64* ki = rows + (size_t)i * W;
+  auto L = [&](long j) -> int {
+    if (j < 0 || j >= (long)m) return -1;
+    return row_lcp<W>(ki, rows + (size_t)j * W);
+  };
+  const int d = (L(i + 1) - L(i - 1)) > 0 ? 1 : -1;
+  const int dmin = L(i - d);
+  long lmax = 2;
+  while (L(i + lmax * d) > dmin) lmax <<= 1;
+  long l = 0;
+  for (long t = lmax >> 1; t >= 1; t >>= 1)
+    if (L(i + (l + t) * d) > dmin) l += t;
+  const long j = i + l * d;
+  const int dnode = L(j);
+  long s = 0, t = l;
+  do {
+    t = (t + 1) >> 1;
+    if (L(i + (s + t) * d) > dnode) s += t;
+  } while (t > 1);
+  const long g = i + s * d + (d < 0 ? -1 : 0);
+  gamma[i] = (u32)g;
+  split[i] = (u32)dnode;
+}
+
+void launch_trie_build(int W, const u64* rows, u32 m, u32* gamma, u32* split, cudaStream_t s) {
+  if (m < 2) return;
+  SW_DISPATCH_W(W, (k_trie_build<WW><<<(m - 1 + 255) / 256, 256, 0, s>>>(rows, m, gamma, split)));
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Tree-walking subset query.  One thread per query row c; a depth-first walk
+// of the radix tree prunes (a) a subtree whose common key prefix has a state
+// that c lacks and (b) every right child (bit set) when c lacks the split
+// bit.  Ranges of at most kLeaf keys are tested directly.  The stack is
+// bounded; a range that does not fit is scanned linearly instead, so the walk
+// is exact for any tree depth.
+// ===========================================================================
+namespace {
+constexpr int kLeaf = 8;
+constexpr int kStack = 40;
+}  // namespace
+
+template <int W, int MODE>
+__global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u32 m, const u32* __restrict__ gamma,
+                                                    const u32* __restrict__ split, const u64* __restrict__ Q, u32 q,
+                                                    int n, u32* __restrict__ flags, u32* witness, int stop) {
+  const u32 qi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= q) return;
+  if (stop && *(volatile u32*)witness) return;
+  u64 c[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    c[w] = Q[(size_t)qi * W + w];
+    if (MODE == kQueryDisjoint) c[w] = ~c[w] & valid_mask(n, w);
+  }
+  auto test = [&](u32 idx) -> bool {
+    const u64* s = S + (size_t)idx * W;
+    bool eq = true;
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      const u64 sv = s[w];
+      if (sv & ~c[w]) return false;
+      eq = eq && (sv == c[w]);
+    }
+    return MODE == kQueryProperSubset ? !eq : true;
+  };
+  bool hit = false;
+  u32 hit_idx = 0;
+  auto scan = [&](u32 lo, u32 hi) {
+    for (u32 x = lo; x <= hi; ++x)
+      if (test(x)) {
+        hit = true;
+        hit_idx = x;
+        return;
+      }
+  };
+  if (m == 0) {
+  } else if (m <= (u32)kLeaf) {
+    scan(0, m - 1);
+  } else {
+    u32 st_node[kStack], st_lo[kStack], st_hi[kStack];
+    int sp = 0;
+    st_node[0] = 0;
+    st_lo[0] = 0;
+    st_hi[0] = m - 1;
+    sp = 1;
+    int iter = 0;
+    while (sp > 0 && !hit) {
+      --sp;
+      const u32 x = st_node[sp], lo = st_lo[sp], hi = st_hi[sp];
+      if (hi - lo + 1 <= (u32)kLeaf) {
+        scan(lo, hi);
+        continue;
+      }
+      if (stop && ((++iter & 31) == 0) && *(volatile u32*)witness) return;
+      const u32 g = gamma[x], b = split[x];
+      // (a) common prefix bits [0, b) of the range must lie inside c
+      bool ok = true;
+      const u64* s = S + (size_t)lo * W;
+#pragma unroll
+      for (int w = 0; w < W; ++w) {
+        const int base = w * 64;
+        if ((int)b > base) {
+          const u64 mask = ((int)b >= base + 64) ? ~0ULL : (~0ULL << (64 - ((int)b - base)));
+          if (s[w] & mask & ~c[w]) ok = false;
+        }
+      }
+      if (!ok) continue;
+      // (b) right child only if c has bit b
+      u64 cw = 0;
+#pragma unroll
+      for (int w = 0; w < W; ++w)
+        if (w == (int)(b >> 6)) cw = c[w];
+      const bool cb = (b < (u32)(W * 64)) && ((cw >> (63 - (b & 63))) & 1ULL);
+      if (cb) {
+        if (sp < kStack) {
+          st_node[sp] = g + 1;
+          st_lo[sp] = g + 1;
+          st_hi[sp] = hi;
+          ++sp;
+        } else {
+          scan(g + 1, hi);
+          if (hit) break;
+        }
+      }
+      if (sp < kStack) {
+        st_node[sp] = g;
+        st_lo[sp] = lo;
+        st_hi[sp] = g;
+        ++sp;
+      } else {
+        scan(lo, g);
+      }
+    }
+  }
+  if (!hit) return;
+  if (stop) {
+    if (atomicCAS(witness, 0u, 1u) == 0u) {
+      witness[1] = qi;
+      witness[2] = hit_idx;
+    }
+  } else {
+    flags[qi] = 1u;
+  }
+}
+
+void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q, u32 q,
+                       int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s) {
+  if (!q || !m) return;
+  const u32 blocks = (q + 127) / 128;
+#define SW_Q(WW)                                                                                                  \
+  case WW:                                                                                                        \
+    if (mode == kQuerySubset)                                                                                     \
+      k_trie_query<WW, kQuerySubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness, stop_at_first); \
+    else if (mode == kQueryProperSubset)                                                                          \
+      k_trie_query<WW, kQueryProperSubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,   \
+                                                                  stop_at_first);                                 \
+    else                                                                                                          \
+      k_trie_query<WW, kQueryDisjoint><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,       \
+                                                              stop_at_first);                                     \
+    break;
+  switch (W) {
+    SW_Q(1)
+    SW_Q(2)
+    SW_Q(4)
+    SW_Q(8)
+    default:
+      throw std::runtime_error("trie query: unsupported width");
+  }
+#undef SW_Q
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Merge of two sorted disjoint row arrays: each element finds its output
+// position by a binary search in the other array (merge path per element).
+// ===========================================================================
+template <int W>
+__global__ void k_merge(const u64* __restrict__ A, u32 na, const u64* __restrict__ B, u32 nb, u64* __restrict__ out) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= na + nb) return;
+  const bool fromA = i < na;
+  const u64* x = fromA ? A + (size_t)i * W : B + (size_t)(i - na) * W;
+  const u64* other = fromA ? B : A;
+  u32 lo = 0, hi = fromA ? nb : na;
+  while (lo < hi) {
+    u32 mid = (lo + hi) >> 1;
+    if (row_less<W>(other + (size_t)mid * W, x)) lo = mid + 1;
+    else hi = mid;
+  }
+  const size_t pos = (size_t)(fromA ? i : i - na) + lo;
+#pragma unroll
+  for (int w = 0; w < W; ++w) out[pos * W + w] = x[w];
+}
+
+void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s) {
+  if (na + nb == 0) return;
+  SW_DISPATCH_W(W, (k_merge<WW><<<(na + nb + 255) / 256, 256, 0, s>>>(A, na, B, nb, out)));
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Gathers and beam keys.
+// ===========================================================================
+__global__ void k_iota(u32* p, u32 m) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) p[i] = i;
+}
+
+template <int W>
+__global__ void k_gather_rows(const u64* __restrict__ src, const u32* __restrict__ idx, u32 m, u64* __restrict__ dst) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const u64* s = src + (size_t)idx[i] * W;
+#pragma unroll
+  for (int w = 0; w < W; ++w) dst[(size_t)i * W + w] = s[w];
+}
+
+// key = [n - |S|, reference-layout words...]: sorting keys ascending orders
+// sets by cardinality descending, ties by the reference's raw word order
+// (Subset::comp_fast, subset.hpp:78-84; the reference's words are the
+// bit-reversed device words).
+template <int W>
+__global__ void k_beam_keys(const u64* __restrict__ rows, u32 m, int n, int R, u64* __restrict__ keys) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  u32 c = 0;
+  u64 r[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    r[w] = rows[(size_t)i * W + w];
+    c += __popcll(r[w]);
+  }
+  keys[(size_t)i * R] = (u64)(n - (int)c);
+#pragma unroll
+  for (int w = 0; w < W; ++w)
+    if (w + 1 < R) keys[(size_t)i * R + 1 + w] = __brevll(r[w]);
+}
+
+void launch_iota(u32* p, u32 m, cudaStream_t s) {
+  if (!m) return;
+  k_iota<<<(m + 255) / 256, 256, 0, s>>>(p, m);
+  SW_LAUNCH_CHECK();
+}
+
+void launch_gather_rows(int W, const u64* src, const u32* idx, u32 m, u64* dst, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_gather_rows<WW><<<(m + 255) / 256, 256, 0, s>>>(src, idx, m, dst)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_beam_keys(int W, const u64* rows, u32 m, int n, int R, u64* keys, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_beam_keys<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, n, R, keys)));
+  SW_LAUNCH_CHECK();
+}
+
+}  // namespace sw

@@ -1,0 +1,95 @@
+// Launchers for the device kernels of the exact search (kernels.cu).
+//
+// Every launcher is asynchronous on the given stream; scratch buffers come
+// from the caller (no allocation inside).  Kernel roles and the reference
+// functions they replace:
+//   expand        PreprocessedTransition::apply
+//                 (synchrolib/data_structures/preprocessed_transitions.cpp:56-93,
+//                  cuda/preprocessed_transition_kernel.cu:19-88)
+//   radix sort +  sort_keep_unique (synchrolib/utils/vector.hpp:13-27)
+//   unique
+//   trie build +  SubsetsImplicitTrie::check_contains_subset / reduce
+//   trie query    (synchrolib/data_structures/subsets_implicit_trie.hpp:29-266,
+//                  cuda/subsets_implicit_trie_kernel.cu:13-92) and
+//                 SubsetsTrie::contains_subset_of (subsets_trie.hpp:78-90)
+#pragma once
+#include "common.cuh"
+
+namespace sw {
+
+// Per-letter transition tables as staged into shared memory by `expand`.
+// Layout (all u16): delta[a*n + q]; inv_beg[a*(n+1) + t] ..inv_beg[..+1] index
+// inv_src[a*n + e] (CSR of preimages).
+struct TransTables {
+  const uint16_t* delta = nullptr;   // k*n
+  const uint16_t* inv_beg = nullptr; // k*(n+1)
+  const uint16_t* inv_src = nullptr; // k*n
+  int n = 0, k = 0;
+};
+
+// out[(a*m + i)] = image (kImage) or preimage of in[i] under letter a.
+void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s);
+
+// Scratch sizing for the sort / scan helpers.
+size_t scan_temp_bytes(u32 n);
+size_t sort_temp_bytes(int R, u32 m);
+
+// Exclusive prefix sum of in[0..n) into out; *total_dev receives the sum.
+void launch_scan(const u32* in, u32* out, u32 n, u32* total_dev, void* temp, cudaStream_t s);
+
+// Stable LSD radix sort of m rows of R words (word 0 most significant) with
+// a u32 payload.  Result lands in (keys, vals); (keys_alt, vals_alt) are
+// scratch of the same size.  `bitmask_dev` (R words) must hold the OR^AND of
+// all rows if `have_mask`, else it is computed here.
+void radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp,
+                     cudaStream_t s);
+
+// flags[i] = 1 if row i differs from row i-1 (rows sorted).
+void launch_unique_flags(int W, const u64* rows, u32 m, u32* flags, cudaStream_t s);
+
+// Stream compaction of rows (+ optional payload) by flags; pos = exclusive scan of flags.
+void launch_compact(int W, const u64* rows, const u32* vals, const u32* flags, const u32* pos, u32 m, u64* out_rows,
+                    u32* out_vals, cudaStream_t s);
+
+// Binary radix tree (Karras 2012) over m >= 2 sorted unique rows: node i in
+// [0, m-2] gets its split position gamma[i] and the first differing bit
+// split[i] of its key range.
+void launch_trie_build(int W, const u64* rows, u32 m, u32* gamma, u32* split, cudaStream_t s);
+
+enum QueryMode : int {
+  kQuerySubset = 0,        // hit(c) = exists s in S, s ⊆ c
+  kQueryProperSubset = 1,  // hit(c) = exists s in S, s ⊊ c
+  kQueryDisjoint = 2,      // hit(c) = exists s in S, s ∩ c = ∅  (s ⊆ ~c)
+};
+
+// Trie query: for each query row c, flags[c] |= hit(c) (or, with
+// `stop_at_first`, record one witness pair and let all threads exit early).
+// witness[0] = found flag, witness[1] = query index, witness[2] = set index.
+void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q,
+                       u32 q, int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s);
+
+// out = sorted merge of two sorted, mutually disjoint row arrays.
+void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);
+
+// rows[i] = complement of rows[i] within n states.
+void launch_complement(int W, u64* rows, u32 m, int n, cudaStream_t s);
+
+// out[i] = popcount of row i.
+void launch_popcount(int W, const u64* rows, u32 m, u32* out, cudaStream_t s);
+
+// flags[i] = AND/OR combine: out[i] = (a[i] == 0 && b[i] == 0).
+void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t s);
+
+// p[i] = i.
+void launch_iota(u32* p, u32 m, cudaStream_t s);
+
+// dst[i] = src[idx[i]] (rows of W words).
+void launch_gather_rows(int W, const u64* src, const u32* idx, u32 m, u64* dst, cudaStream_t s);
+
+// Beam sort keys: keys[i] = [n - |row i|, bit-reversed words of row i] (R words).
+void launch_beam_keys(int W, const u64* rows, u32 m, int n, int R, u64* keys, cudaStream_t s);
+
+// Fill u32 array with a value.
+void launch_fill_u32(u32* p, u32 value, u32 m, cudaStream_t s);
+
+}  // namespace sw

@@ -1,0 +1,132 @@
+"""Exact / Beam parity on the GPU against the oracle (the CPU restatement of the
+reference, itself pinned to the compiled reference) and word verification."""
+import json
+
+import pytest
+
+import oracle
+from synchrowords_gb300.generate import cerny, hard, random_dfa, slowlysink
+
+pytestmark = pytest.mark.gpu
+
+EXACT = json.dumps({"algorithms": [{"name": "Exact", "config": {}}]})
+BEAM_EXACT = json.dumps({
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1",
+    "algorithms": [
+        {"name": "Beam", "config": {"presort": "indeg", "dynamic": True,
+                                    "min_beam_size": "AUT_N * std::log2(AUT_N)",
+                                    "max_beam_size": "AUT_N * AUT_N * std::log2(AUT_N)",
+                                    "beam_exact_ratio": 0.01}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "max_memory_mb": "12 * 1024"}}]})
+
+
+def check_word(d, n, k, r):
+    assert r.word is not None, "no word returned"
+    assert len(r.word) == r.upper
+    assert all(0 <= a < k for a in r.word)
+    assert len(oracle.apply_word(d, n, k, r.word)) == 1
+
+
+@pytest.mark.parametrize("seed", range(1, 17))
+def test_random_n48_exact(ctx, seed):
+    n, k = 48, 2
+    d = random_dfa(n, k, seed)
+    r = ctx.solve(d, n, k, EXACT)
+    ref = oracle.exact(d, n, k)
+    assert (r.lower, r.upper) == (ref.lower, ref.upper)
+    check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("n", [2, 3, 4, 5, 8, 12, 20, 28])
+def test_cerny(ctx, n):
+    d = cerny(n)
+    r = ctx.solve(d, n, 2, EXACT)
+    assert r.lower == r.upper == (n - 1) ** 2
+    check_word(d, n, 2, r)
+
+
+@pytest.mark.parametrize("n", [10, 11, 12, 13, 14, 15, 16, 17, 18, 19, 20])
+def test_generate_hard_known_answers(ctx, n):
+    # automaton.hpp:97-101
+    expected = dict(zip(range(10, 21), [29, 35, 40, 44, 49, 54, 59, 63, 69, 76, 82]))[n]
+    d = hard(n)
+    r = ctx.solve(d, n, 2, EXACT)
+    assert r.lower == r.upper == expected
+    check_word(d, n, 2, r)
+
+
+@pytest.mark.parametrize("n", [3, 4, 5, 6, 7])
+def test_slowly_synchronizing_sink(ctx, n):
+    d = slowlysink(n)
+    r = ctx.solve(d, n, n - 1, EXACT)
+    assert r.lower == r.upper == n * (n - 1) // 2
+    check_word(d, n, n - 1, r)
+
+
+@pytest.mark.parametrize("seed", range(1, 25))
+def test_small_random_vs_brute(ctx, seed):
+    n = 6 + seed % 12
+    k = 2 + seed % 3
+    d = random_dfa(n, k, 500 + seed)
+    truth = oracle.brute(d, n, k)
+    r = ctx.solve(d, n, k, EXACT)
+    if truth < 0:
+        assert r.non_synchro
+    else:
+        assert (r.lower, r.upper) == (truth, truth)
+        check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3, 4])
+def test_random_n200_exact(ctx, seed):
+    n, k = 200, 2
+    d = random_dfa(n, k, seed)
+    r = ctx.solve(d, n, k, EXACT)
+    ref = oracle.exact(d, n, k, oracle.ExactParams(threads=4))
+    assert (r.lower, r.upper) == (ref.lower, ref.upper)
+    check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("seed", [5, 6])
+def test_random_n200_beam_exact(ctx, seed):
+    n, k = 200, 2
+    d = random_dfa(n, k, seed)
+    r = ctx.solve(d, n, k, BEAM_EXACT)
+    import math
+    lg = math.log2(n)
+    b = oracle.beam(d, n, k, oracle.BeamParams(dynamic=True, presort_indeg=True, min_beam_size=int(n * lg),
+                                               max_beam_size=int(n * n * lg)), upper=(n - 1) ** 2 + 1)
+    ex = oracle.exact(d, n, k, oracle.ExactParams(dfs_min_list_size=8192, bfs_small_list_size=n * k,
+                                                  max_memory_mb=12 * 1024, threads=4), upper=b.upper)
+    assert (r.lower, r.upper) == (ex.lower, ex.upper)
+    check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+@pytest.mark.parametrize("dynamic", [False, True])
+def test_beam_bound_matches_reference(ctx, seed, dynamic):
+    import math
+    n, k = 100, 3
+    d = random_dfa(n, k, 70 + seed)
+    lg = math.log2(n)
+    cfg = {"presort": "indeg", "dynamic": dynamic, "beam_size": "AUT_N * std::log2(AUT_N)"}
+    plan = json.dumps({"algorithms": [{"name": "Beam", "config": cfg}]})
+    r = ctx.solve(d, n, k, plan)
+    b = oracle.beam(d, n, k, oracle.BeamParams(beam_size=int(n * lg), dynamic=dynamic, presort_indeg=True))
+    assert r.upper == b.upper
+    if r.word is not None:
+        check_word(d, n, k, r)
+
+
+def test_non_synchronizing(ctx):
+    # two disjoint cycles: no reset word
+    n, k = 6, 2
+    d = [1, 1, 2, 2, 0, 0, 4, 4, 5, 5, 3, 3]
+    r = ctx.solve(d, n, k, EXACT)
+    assert r.non_synchro
+
+
+def test_single_state(ctx):
+    r = ctx.solve([0, 0, 0, 0], 1, 4, EXACT)
+    assert (r.lower, r.upper) == (0, 0)
