@@ -1,0 +1,318 @@
+#!/usr/bin/env python3
+"""Benchmark: time-to-exact reset length per random DFA on one GB300.
+
+Workload (default, `--workload n200`): 16 random binary DFAs, n = 200 states,
+k = 2 letters, transitions uniform from SplitMix64 seeds, solved with the
+reference's plain Exact plan (`{"algorithms": [{"name": "Exact"}]}`, default
+upper bound n^3/6).  One step = solving all 16 DFAs through the public API.
+The reference has no public benchmark suite; these seeded synthetic automata
+stand in with the shapes its configs name.
+
+Printed JSON line (rank 0):
+  value     ms per DFA from CUDA events on the library's stream (max over ranks)
+  e2e       ms per DFA by wall clock around the public call (host automaton in,
+            bounds + word out)
+  roofline  the kernel class with the most device time in one profiled step:
+            algorithmic bytes / event-timed duration vs measured HBM peak
+  cpu_baseline  the oracle (CPU restatement of the reference, oracle/) on a
+            bounded sample of the same DFAs, all host threads
+
+`--impl reference` times that CPU restatement alone (rank 0; other ranks exit).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PLAN_EXACT = json.dumps({"algorithms": [{"name": "Exact", "config": {}}]})
+
+WORKLOADS = {
+    # name: (n, k, count, description)
+    "n200": (200, 2, 16, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
+    "n48": (48, 2, 64, "plain exact, 64 random binary DFAs, n=48 (64-bit sets)"),
+}
+
+
+def workload_dfas(name: str, rank: int):
+    from synchrowords_gb300.generate import random_dfa
+    n, k, count, _ = WORKLOADS[name]
+    base = 1 + rank * 100000
+    return [(n, k, random_dfa(n, k, base + i)) for i in range(count)]
+
+
+def load_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = ROOT / "profiles" / "traffic.json"
+    if p.exists():
+        try:
+            return json.loads(p.read_text())
+        except Exception:
+            return {}
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.samples = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except Exception:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def summary(self):
+        if not getattr(self, "samples", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier_max(value: float, world: int) -> float:
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline(dfas, sample: int, threads: int):
+    """Oracle (CPU restatement of the reference's Exact) on the first `sample` DFAs."""
+    import oracle
+    oracle.build()
+    t0 = time.perf_counter()
+    lengths = []
+    for n, k, d in dfas[:sample]:
+        r = oracle.exact(d, n, k, oracle.ExactParams(threads=threads))
+        lengths.append(r.upper)
+    dt = time.perf_counter() - t0
+    return dt * 1000.0 / sample, lengths
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    dfas = workload_dfas(args.workload, 0)
+    threads = max(1, min(64, os.cpu_count() or 1))
+    per_step = max(1, min(len(dfas), args.ref_sample))
+    for w in range(args.warmup):
+        cpu_baseline(dfas[w % len(dfas):] + dfas, 1, threads)
+    times = []
+    for s in range(args.steps):
+        sub = [dfas[(s * per_step + i) % len(dfas)] for i in range(per_step)]
+        ms, _ = cpu_baseline(sub, per_step, threads)
+        times.append(ms)
+    value = sum(times) / len(times)
+    n, k, count, desc = WORKLOADS[args.workload]
+    line = {
+        "impl": "reference", "metric": "time-to-exact reset length per random DFA", "value": round(value, 4),
+        "unit": "ms", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(value * per_step, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step": per_step, "plan": "Exact (defaults)",
+                   "l2": "host-only run"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} DFAs per step out of {count}, rotating"},
+        "e2e": {"value": round(value, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+    import synchrowords_gb300 as sw
+    from synchrowords_gb300 import build as nb
+    nb.build()
+    torch.cuda.set_device(local)
+    dfas = workload_dfas(args.workload, rank)
+    n, k, count, desc = WORKLOADS[args.workload]
+    ctx = sw.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def one_step():
+        launches = 0
+        lengths = []
+        for r in ctx.solve_batch(dfas, PLAN_EXACT, workers=args.streams):
+            launches += r.stats["kernel_launches"]
+            lengths.append(r.upper)
+            if r.word is None or len(r.word) != r.upper:
+                raise RuntimeError("solve returned no verified word")
+        return launches, lengths
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    dev_ms, wall_ms, launches = [], [], 0
+    lengths = None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            barrier(world)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            t0 = time.perf_counter()
+            l, lengths = one_step()
+            t1 = time.perf_counter()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            launches += l
+            dev_ms.append(e0.elapsed_time(e1))
+            wall_ms.append((t1 - t0) * 1000.0)
+    barrier(world)
+    dev_total = barrier_max(sum(dev_ms), world)
+    wall_total = barrier_max(sum(wall_ms), world)
+    total_dfas = args.steps * count * world
+    value = dev_total / (args.steps * count)  # per-rank DFAs run concurrently on separate GPUs
+    value_job = dev_total / total_dfas
+    e2e = wall_total / total_dfas
+
+    # one extra, untimed step with per-kernel-class CUDA-event profiling
+    flush.zero_()
+    torch.cuda.synchronize()
+    ctx.profile_begin()
+    pairs = 0
+    for (nn, kk, d) in dfas:
+        r = ctx.solve(d, nn, kk, PLAN_EXACT)
+        pairs += r.stats["logical_pairs"]
+    prof = ctx.profile_end()
+    peak, peak_kind = load_peaks()
+    top = max(prof, key=lambda c: prof[c]["ms"])
+    p = prof[top]
+    achieved = (p["bytes"] / 1e9) / (p["ms"] / 1e3) if p["ms"] > 0 else 0.0
+    traffic = load_traffic().get(f"{args.workload}:{top}")
+    roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 5), "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": round(p["bytes"] / max(1, p["launches"]), 1),
+                "avg_launch_us": round(1000.0 * p["ms"] / max(1, p["launches"]), 3),
+                "traffic": traffic,
+                "classes": {c: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                                "GB/s": round((v["bytes"] / 1e9) / (v["ms"] / 1e3), 2) if v["ms"] > 0 else 0.0}
+                            for c, v in prof.items()}}
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        threads = max(1, min(64, os.cpu_count() or 1))
+        sample = min(args.cpu_sample, count)
+        cpu_ms, cpu_len = cpu_baseline(dfas, sample, threads)
+        if cpu_len != lengths[:sample]:
+            raise RuntimeError(f"length mismatch vs oracle: {cpu_len} != {lengths[:sample]}")
+        cpu = {"value": round(cpu_ms, 3), "unit": "ms", "cores": threads, "kind": "port",
+               "sample": f"first {sample} of the {count} DFAs, oracle Exact with {threads} threads"}
+    h2d = sum(4 * nn * kk for nn, kk, _ in dfas)
+    d2h = sum(4 * (L + 8) for L in lengths)
+    line = {
+        "metric": "time-to-exact reset length per random DFA", "value": round(value_job, 4), "unit": "ms",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dev_total / args.steps, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": "Exact (defaults)",
+                   "streams": args.streams,
+                   "l2": "flushed (256 MB write) before every timed step", "per_gpu_ms_per_dfa": round(value, 4)},
+        "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": roofline,
+        "subset_check_pairs_per_s": round(pairs / (sum(v["ms"] for v in prof.values()) / 1e3), 1) if prof else None,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "lengths": lengths,
+    }
+    if cpu is not None:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="n200")
+    ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--ref-sample", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -158,6 +158,36 @@ int sw_solve(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, con
 int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const char* plan_json,
                   sw_result* result);
 
+/* Solve `count` automata with the same plan (evaluated per automaton's n, k).
+ * deltas holds the automata back to back (n_i*k_i entries each); results[i]
+ * gets instance i (set results[i].word / word_capacity beforehand to receive
+ * words).  `workers` device streams (0 = min(count, 16)), each driven by its
+ * own host thread, solve instances concurrently on the context's GPU.  The
+ * reference solves the automata of a file one after another
+ * (app/main.cpp:48-78); there is no batched counterpart. */
+int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                   const char* plan_json, sw_result* results, uint32_t workers);
+
+/* ---- measurement --------------------------------------------------------
+ * No counterpart in the reference (its timers are host RAII timers,
+ * synchrolib/utils/timer.hpp:9-41).  Between sw_profile_begin and
+ * sw_profile_end every kernel launch of the context is bracketed by CUDA
+ * events on the context's stream; sw_profile_end synchronises and reports, per
+ * kernel class, the launches, summed device milliseconds and the algorithmic
+ * bytes those launches had to move.  Classes: 0 subset-query tree walks,
+ * 1 layer expansion, 2 radix sorts, 3 everything else. */
+typedef struct {
+  uint64_t launches;
+  double ms;
+  double bytes;
+} sw_kernel_profile;
+
+#define SW_PROFILE_CLASSES 4
+int sw_profile_begin(sw_context* ctx);
+int sw_profile_end(sw_context* ctx, sw_kernel_profile out[SW_PROFILE_CLASSES]);
+/* The cudaStream_t (as void*) every kernel of `ctx` is launched on. */
+void* sw_context_stream(sw_context* ctx);
+
 /* ---- kernel-level entry points (host buffers, reference bitset layout) ---
  * These are the device operations the reference offloads, exposed for parity
  * tests and for callers that drive their own search. */

@@ -80,6 +80,12 @@ class _Result(ctypes.Structure):
                 ("n_runs", ctypes.c_uint32), ("runs", _Run * MAX_ALGOS), ("stats", _Stats)]
 
 
+class _KernelProfile(ctypes.Structure):
+    _fields_ = [("launches", ctypes.c_uint64), ("ms", ctypes.c_double), ("bytes", ctypes.c_double)]
+
+
+PROFILE_CLASSES = ("subset_query", "expand", "radix_sort", "other")
+
 _lib = None
 
 _U32P = ctypes.POINTER(ctypes.c_uint32)
@@ -112,6 +118,12 @@ def load_library():
     lib.sw_subsets_check.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P,
                                      ctypes.c_uint64, ctypes.c_int32, ctypes.POINTER(ctypes.c_uint8)]
     lib.sw_sort_unique.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P]
+    lib.sw_solve_batch.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
+                                   ctypes.POINTER(_Result), ctypes.c_uint32]
+    lib.sw_profile_begin.argtypes = [ctypes.c_void_p]
+    lib.sw_profile_end.argtypes = [ctypes.c_void_p, ctypes.POINTER(_KernelProfile)]
+    lib.sw_context_stream.argtypes = [ctypes.c_void_p]
+    lib.sw_context_stream.restype = ctypes.c_void_p
     _lib = lib
     return lib
 
@@ -200,6 +212,49 @@ class Context:
         runs = [(r.runs[i].name.decode(), r.runs[i].ms) for i in range(r.n_runs)]
         stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
         return Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats)
+
+    def solve_batch(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
+                    workers: int = 0) -> List[Result]:
+        """Solve many automata concurrently (one device stream per worker)."""
+        count = len(automata)
+        if count == 0:
+            return []
+        ns = _u32([a[0] for a in automata])
+        ks = _u32([a[1] for a in automata])
+        deltas = _u32([x for a in automata for x in a[2]])
+        res = (_Result * count)()
+        bufs = []
+        for i, (n, k, _) in enumerate(automata):
+            cap = max(1 << 12, 4 * n * n)
+            b = np.zeros(cap, dtype=np.uint32)
+            bufs.append(b)
+            res[i].word = b.ctypes.data_as(_U32P)
+            res[i].word_capacity = cap
+        _check(self._lib.sw_solve_batch(self._h, count, deltas.ctypes.data_as(_U32P), ns.ctypes.data_as(_U32P),
+                                        ks.ctypes.data_as(_U32P), plan_json.encode(), res, workers))
+        out = []
+        for i in range(count):
+            r = res[i]
+            word = bufs[i][: r.word_len].tolist() if r.has_word else None
+            runs = [(r.runs[j].name.decode(), r.runs[j].ms) for j in range(r.n_runs)]
+            stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
+            out.append(Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats))
+        return out
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t (as an integer) that every kernel of this context uses."""
+        return int(self._lib.sw_context_stream(self._h) or 0)
+
+    def profile_begin(self) -> None:
+        _check(self._lib.sw_profile_begin(self._h))
+
+    def profile_end(self) -> dict:
+        """Per kernel class: launches, device ms (CUDA events) and algorithmic bytes."""
+        arr = (_KernelProfile * len(PROFILE_CLASSES))()
+        _check(self._lib.sw_profile_end(self._h, arr))
+        return {name: {"launches": arr[i].launches, "ms": arr[i].ms, "bytes": arr[i].bytes}
+                for i, name in enumerate(PROFILE_CLASSES)}
 
     # ---- kernel-level entry points (reference bitset layout) ----
     def apply_transition(self, delta, n: int, k: int, letter: int, inverse: bool, sets: np.ndarray) -> np.ndarray:

@@ -1,7 +1,11 @@
 // C ABI (include/synchrowords.h).  Every entry point catches exceptions and
 // turns them into status codes with a thread-local message, where the
 // reference exits or throws across dlopen (app/jit.hpp:61-83).
+#include <atomic>
 #include <chrono>
+#include <mutex>
+#include <thread>
+#include <vector>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -14,6 +18,7 @@
 
 struct sw_context {
   std::unique_ptr<sw::Solver> solver;
+  std::vector<std::unique_ptr<sw::Solver>> workers;  // extra streams for sw_solve_batch
 };
 
 namespace {
@@ -99,50 +104,122 @@ int sw_context_create(int device, sw_context** out) {
 
 void sw_context_destroy(sw_context* ctx) { delete ctx; }
 
+namespace {
+
+// Runs a plan on one automaton with one solver (jit/jitmain.cpp:11-49).
+// Returns SW_OK or an error code; throws on device errors (caught by callers).
+int run_plan(sw::Solver& solver, const uint32_t* delta, uint32_t n, uint32_t k, const sw_plan* plan, sw_result* r,
+             std::string& err) {
+  sw::Automaton A = sw::make_automaton(delta, n, k);
+  uint32_t* word_buf = r->word;
+  uint32_t word_cap = r->word_capacity;
+  std::memset(r, 0, sizeof(*r));
+  r->word = word_buf;
+  r->word_capacity = word_cap;
+  // jit/jitmain.cpp:21-32 — bounds start at [0, min(UPPER_BOUND, max)]
+  sw::Bounds b;
+  b.lower = 0;
+  b.upper = plan->upper_bound;
+  if (plan->n_algorithms > SW_MAX_ALGORITHMS) {
+    err = "too many algorithms";
+    return SW_ERR_CONFIG;
+  }
+  for (uint32_t i = 0; i < plan->n_algorithms; ++i) {
+    const sw_algorithm& alg = plan->algorithms[i];
+    auto t0 = std::chrono::steady_clock::now();
+    switch (alg.kind) {
+      case SW_ALGO_EXACT:
+        solver.exact(A, alg.exact, b, r->stats);
+        break;
+      case SW_ALGO_BEAM:
+        solver.beam(A, alg.beam, b, r->stats);
+        break;
+      default:
+        err = std::string("algorithm ") + alg.name + " is outside this library's scope (supported: Exact, Beam)";
+        return SW_ERR_UNSUPPORTED;
+    }
+    auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
+    set_name(r->runs[r->n_runs].name, alg.name);
+    r->runs[r->n_runs].ms = (uint64_t)ms;
+    r->n_runs++;
+  }
+  r->non_synchro = b.non_synchro ? 1 : 0;
+  r->mlsw_lower_bound = b.lower;
+  r->mlsw_upper_bound = b.upper;
+  if (b.has_word && b.word.size() == b.upper && !b.non_synchro) {
+    r->has_word = 1;
+    r->word_len = (uint32_t)b.word.size();
+    if (r->word) {
+      if (r->word_capacity < b.word.size()) {
+        err = "word buffer too small";
+        return SW_ERR_CAPACITY;
+      }
+      std::memcpy(r->word, b.word.data(), sizeof(uint32_t) * b.word.size());
+    }
+  }
+  return SW_OK;
+}
+
+}  // namespace
+
 int sw_solve(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const sw_plan* plan, sw_result* r) {
   if (!ctx || !plan || !r) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
   return guarded([&] {
-    sw::Automaton A = sw::make_automaton(delta, n, k);
-    uint32_t* word_buf = r->word;
-    uint32_t word_cap = r->word_capacity;
-    std::memset(r, 0, sizeof(*r));
-    r->word = word_buf;
-    r->word_capacity = word_cap;
-    // jit/jitmain.cpp:21-32 — bounds start at [0, min(UPPER_BOUND, max)]
-    sw::Bounds b;
-    b.lower = 0;
-    b.upper = plan->upper_bound;
-    if (plan->n_algorithms > SW_MAX_ALGORITHMS) return fail(SW_ERR_CONFIG, "too many algorithms");
-    for (uint32_t i = 0; i < plan->n_algorithms; ++i) {
-      const sw_algorithm& alg = plan->algorithms[i];
-      auto t0 = std::chrono::steady_clock::now();
-      switch (alg.kind) {
-        case SW_ALGO_EXACT:
-          ctx->solver->exact(A, alg.exact, b, r->stats);
-          break;
-        case SW_ALGO_BEAM:
-          ctx->solver->beam(A, alg.beam, b, r->stats);
-          break;
-        default:
-          return fail(SW_ERR_UNSUPPORTED, std::string("algorithm ") + alg.name +
-                                              " is outside this library's scope (supported: Exact, Beam)");
+    std::string err;
+    int rc = run_plan(*ctx->solver, delta, n, k, plan, r, err);
+    return rc == SW_OK ? SW_OK : fail(rc, err);
+  });
+}
+
+int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                   const char* plan_json, sw_result* results, uint32_t workers) {
+  if (!ctx || !plan_json || (count && (!deltas || !ns || !ks || !results)))
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    if (count == 0) return SW_OK;
+    std::vector<size_t> off(count + 1, 0);
+    for (uint32_t i = 0; i < count; ++i) off[i + 1] = off[i] + (size_t)ns[i] * ks[i];
+    if (workers == 0) workers = std::min<uint32_t>(count, 16);
+    workers = std::max<uint32_t>(1, std::min<uint32_t>(workers, count));
+    while (ctx->workers.size() + 1 < workers)
+      ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
+    std::atomic<uint32_t> next{0};
+    std::atomic<int> first_rc{SW_OK};
+    std::mutex err_mu;
+    std::string first_err;
+    auto work = [&](sw::Solver& solver) {
+      uint32_t i;
+      while ((i = next++) < count && first_rc.load() == SW_OK) {
+        int rc;
+        std::string err;
+        try {
+          sw_plan plan;
+          sw::plan_from_json(plan_json, ns[i], ks[i], &plan);
+          rc = run_plan(solver, deltas + off[i], ns[i], ks[i], &plan, &results[i], err);
+        } catch (const sw::CudaError& e) {
+          rc = SW_ERR_CUDA;
+          err = e.what();
+        } catch (const std::invalid_argument& e) {
+          rc = SW_ERR_INVALID_ARGUMENT;
+          err = e.what();
+        } catch (const std::exception& e) {
+          rc = SW_ERR_INTERNAL;
+          err = e.what();
+        }
+        if (rc != SW_OK) {
+          std::lock_guard<std::mutex> g(err_mu);
+          if (first_rc.load() == SW_OK) {
+            first_rc = rc;
+            first_err = "instance " + std::to_string(i) + ": " + err;
+          }
+        }
       }
-      auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
-      set_name(r->runs[r->n_runs].name, alg.name);
-      r->runs[r->n_runs].ms = (uint64_t)ms;
-      r->n_runs++;
-    }
-    r->non_synchro = b.non_synchro ? 1 : 0;
-    r->mlsw_lower_bound = b.lower;
-    r->mlsw_upper_bound = b.upper;
-    if (b.has_word && b.word.size() == b.upper && !b.non_synchro) {
-      r->has_word = 1;
-      r->word_len = (uint32_t)b.word.size();
-      if (r->word) {
-        if (r->word_capacity < b.word.size()) return fail(SW_ERR_CAPACITY, "word buffer too small");
-        std::memcpy(r->word, b.word.data(), sizeof(uint32_t) * b.word.size());
-      }
-    }
+    };
+    std::vector<std::thread> th;
+    for (uint32_t w = 1; w < workers; ++w) th.emplace_back(work, std::ref(*ctx->workers[w - 1]));
+    work(*ctx->solver);
+    for (auto& t : th) t.join();
+    if (first_rc.load() != SW_OK) return fail(first_rc.load(), first_err);
     return SW_OK;
   });
 }
@@ -154,6 +231,24 @@ int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k
   if (rc != SW_OK) return rc;
   return sw_solve(ctx, delta, n, k, &plan, r);
 }
+
+int sw_profile_begin(sw_context* ctx) {
+  if (!ctx) return fail(SW_ERR_INVALID_ARGUMENT, "NULL context");
+  return guarded([&] {
+    ctx->solver->profile_begin();
+    return SW_OK;
+  });
+}
+
+int sw_profile_end(sw_context* ctx, sw_kernel_profile out[SW_PROFILE_CLASSES]) {
+  if (!ctx || !out) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    ctx->solver->profile_end(out);
+    return SW_OK;
+  });
+}
+
+void* sw_context_stream(sw_context* ctx) { return ctx ? ctx->solver->stream() : nullptr; }
 
 int sw_apply_transition(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, uint32_t letter,
                         int32_t inverse, const uint64_t* from, uint64_t* to, uint64_t count) {

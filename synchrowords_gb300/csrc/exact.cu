@@ -63,12 +63,75 @@ class Engine {
     SW_CUDA(cudaMalloc(&d_misc, 64 * sizeof(u32)));
   }
   ~Engine() {
+    for (auto e : ev_pool) cudaEventDestroy(e);
+    if (d_query_bytes) cudaFree(d_query_bytes);
     if (d_misc) cudaFree(d_misc);
     if (stream) cudaStreamDestroy(stream);
   }
 
   cudaStream_t stream = nullptr;
   HostPinned pinned;
+
+  // ---- optional per-kernel-class timing (CUDA events on `stream`) ----
+  // class 0: subset-query tree walks, 1: layer expansion, 2: radix sorts,
+  // 3: everything else (unique/compaction/tree build/merge).
+  struct ProfClass {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+    u64 launches = 0;
+    double bytes = 0;
+  };
+  bool prof_on = false;
+  ProfClass prof[4];
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_next = 0;
+  u64* d_query_bytes = nullptr;
+  cudaEvent_t next_event() {
+    if (ev_next == ev_pool.size()) {
+      cudaEvent_t e;
+      SW_CUDA(cudaEventCreate(&e));
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_next++];
+  }
+  template <class Fn>
+  void timed(int cls, double bytes, Fn&& fn) {
+    if (!prof_on) {
+      fn();
+      return;
+    }
+    cudaEvent_t a = next_event(), b = next_event();
+    SW_CUDA(cudaEventRecord(a, stream));
+    fn();
+    SW_CUDA(cudaEventRecord(b, stream));
+    prof[cls].ev.emplace_back(a, b);
+    prof[cls].launches++;
+    prof[cls].bytes += bytes;
+  }
+  void profile_begin() {
+    if (!d_query_bytes) SW_CUDA(cudaMalloc(&d_query_bytes, sizeof(u64)));
+    SW_CUDA(cudaMemsetAsync(d_query_bytes, 0, sizeof(u64), stream));
+    for (auto& c : prof) c = ProfClass{};
+    ev_next = 0;
+    prof_on = true;
+  }
+  void profile_end(sw_kernel_profile out[4]) {
+    SW_CUDA(cudaStreamSynchronize(stream));
+    u64 qb = 0;
+    SW_CUDA(cudaMemcpy(&qb, d_query_bytes, sizeof(u64), cudaMemcpyDeviceToHost));
+    prof[0].bytes += (double)qb;
+    for (int c = 0; c < 4; ++c) {
+      double ms = 0;
+      for (auto& pr : prof[c].ev) {
+        float t = 0;
+        SW_CUDA(cudaEventElapsedTime(&t, pr.first, pr.second));
+        ms += t;
+      }
+      out[c].launches = prof[c].launches;
+      out[c].ms = ms;
+      out[c].bytes = prof[c].bytes;
+    }
+    prof_on = false;
+  }
   u32* d_misc = nullptr;  // [0..3] witness, [8] scan total
   // tables
   DevBuf t_delta, t_beg, t_src;
@@ -110,8 +173,10 @@ class Engine {
     pos.reserve(sizeof(u32) * (size_t)m);
     scan_tmp.reserve(scan_temp_bytes(m));
     u32* total = d_misc + 8;
-    launch_scan(flags, pos.as<u32>(), m, total, scan_tmp.p, stream);
-    launch_compact(W, rows, vals, flags, pos.as<u32>(), m, out_rows, out_vals, stream);
+    timed(3, (double)m * (4 + 4 + 4 + 8.0 * W + 4), [&] {
+      launch_scan(flags, pos.as<u32>(), m, total, scan_tmp.p, stream);
+      launch_compact(W, rows, vals, flags, pos.as<u32>(), m, out_rows, out_vals, stream);
+    });
     count_launch(4);
     return read_u32(total);
   }
@@ -120,24 +185,51 @@ class Engine {
     alt_rows.reserve(sizeof(u64) * R * (size_t)m);
     alt_vals.reserve(sizeof(u32) * (size_t)m);
     sort_tmp.reserve(sort_temp_bytes(R, m));
-    radix_sort_rows(R, rows, vals, alt_rows.as<u64>(), alt_vals.as<u32>(), m, sort_tmp.p, stream);
-    count_launch(3 * 8 * R);
+    int launches = 0;
+    // algorithmic bytes: every pass reads and writes each (row, payload) once
+    // and the upsweep reads one digit word per row
+    timed(2, 0.0, [&] {
+      launches = radix_sort_rows(R, rows, vals, alt_rows.as<u64>(), alt_vals.as<u32>(), m, sort_tmp.p, stream);
+    });
+    const int passes = launches > 1 ? (launches - 1) / 5 : 1;
+    if (prof_on) prof[2].bytes += (double)m * passes * (8.0 + 2.0 * (8.0 * R + 4));
+    count_launch(launches);
   }
 
+  // Subset queries run on the tiled check (subset_check.cu); the radix-tree
+  // walk (kernels.cu) is kept as the alternative engine behind `use_tree`.
+  bool use_tree = false;
+  DevBuf tile_and;
+
   void build_tree(int W, const u64* rows, u32 m, DevBuf& gamma, DevBuf& split) {
-    if (m < 2) return;
+    if (!use_tree || m < 2) return;
     gamma.reserve(sizeof(u32) * m);
     split.reserve(sizeof(u32) * m);
-    launch_trie_build(W, rows, m, gamma.as<u32>(), split.as<u32>(), stream);
+    timed(3, (double)m * (8.0 * W * 2 + 8), [&] {
+      launch_trie_build(W, rows, m, gamma.as<u32>(), split.as<u32>(), stream);
+    });
     count_launch();
   }
 
   void query(int W, int mode, const u64* S, u32 m, const DevBuf& gamma, const DevBuf& split, const u64* Q, u32 q,
              int n, u32* flags, bool stop) {
     if (!m || !q) return;
-    launch_trie_query(W, mode, S, m, m >= 2 ? gamma.as<u32>() : nullptr, m >= 2 ? split.as<u32>() : nullptr, Q, q,
-                      n, flags, d_misc, stop, stream);
-    count_launch();
+    if (use_tree) {
+      timed(0, 0.0, [&] {
+        launch_trie_query(W, mode, S, m, m >= 2 ? gamma.as<u32>() : nullptr, m >= 2 ? split.as<u32>() : nullptr, Q,
+                          q, n, flags, d_misc, stop, stream, prof_on ? d_query_bytes : nullptr);
+      });
+      count_launch();
+    } else {
+      tile_and.reserve(subset_check_temp_bytes(W, m));
+      timed(3, (double)m * 8.0 * W, [&] { launch_tile_and(W, S, m, tile_and.as<u64>(), stream); });
+      // algorithmic bytes: the query rows plus every S tile staged on chip
+      timed(0, (double)q * 8.0 * W, [&] {
+        launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, stream,
+                            prof_on ? d_query_bytes : nullptr);
+      });
+      count_launch(2);
+    }
     if (st) {
       st->trie_queries += q;
       st->logical_pairs += (u64)m * q;
@@ -157,7 +249,10 @@ class Engine {
     flags_a.reserve(sizeof(u32) * N);
     flags_b.reserve(sizeof(u32) * N);
     keep.reserve(sizeof(u32) * N);
-    launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream);
+    // expansion reads each parent row and writes k child rows
+    timed(1, (double)m * 8.0 * W * (1 + k), [&] {
+      launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream);
+    });
     launch_iota(ch_vals.as<u32>(), Nc, stream);
     count_launch(2);
     if (st) st->subsets_expanded += N;
@@ -195,7 +290,9 @@ class Engine {
     X.layers.push_back(std::move(L));
     // visited := visited ∪ layer (both sorted, disjoint)
     X.vis_alt.reserve(sizeof(u64) * W * ((size_t)X.vis_count + f + 1));
-    launch_merge(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
+    timed(3, (double)(X.vis_count + f) * 8.0 * W * 2, [&] {
+      launch_merge(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
+    });
     count_launch();
     std::swap(X.vis.p, X.vis_alt.p);
     std::swap(X.vis.cap, X.vis_alt.cap);
@@ -220,10 +317,47 @@ class Engine {
 Solver::Solver(int device) : device_(device), eng_(new Engine(device)) {}
 Solver::~Solver() = default;
 
+void* Solver::stream() const { return (void*)eng_->stream; }
+void Solver::profile_begin() {
+  SW_CUDA(cudaSetDevice(device_));
+  eng_->profile_begin();
+}
+void Solver::profile_end(sw_kernel_profile out[4]) {
+  SW_CUDA(cudaSetDevice(device_));
+  eng_->profile_end(out);
+}
+
 // ---------------------------------------------------------------------------
 // Exact::run (exact.cpp:37-97) on the device.
 // ---------------------------------------------------------------------------
-void Solver::exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw_stats& st) {
+// State order for the device search: states most likely to lie in forward
+// images first (descending stationary mass of the random walk that applies a
+// uniform random letter, with a 1% uniform restart).  Images are then most
+// often separated by their first word, and the subset check's tile filter
+// sees the shared states of a tile early.  The reference orders by stationary
+// mass too (synchrolib/algorithm/exact/exact.cpp:108-127, ascending there, for
+// its CPU trie); the order changes the work done, never the result.
+static std::vector<uint32_t> image_frequency_order(const Automaton& A) {
+  const uint32_t n = A.n, k = A.k;
+  std::vector<double> pi(n, 1.0 / n), nx(n);
+  for (int it = 0; it < 200; ++it) {
+    std::fill(nx.begin(), nx.end(), 0.01 / n);
+    for (uint32_t q = 0; q < n; ++q) {
+      const double w = 0.99 * pi[q] / k;
+      for (uint32_t a = 0; a < k; ++a) nx[A.at(q, a)] += w;
+    }
+    pi.swap(nx);
+  }
+  std::vector<uint32_t> idx(n);
+  std::iota(idx.begin(), idx.end(), 0u);
+  std::stable_sort(idx.begin(), idx.end(), [&](uint32_t x, uint32_t y) { return pi[x] > pi[y]; });
+  std::vector<uint32_t> order(n);
+  for (uint32_t r = 0; r < n; ++r) order[idx[r]] = r;
+  return order;
+}
+
+void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, sw_stats& st) {
+  const Automaton A = permute(A0, image_frequency_order(A0));
   if (b.non_synchro || b.lower == b.upper) return;  // exact.cpp:45-47
   if (A.n == 1) {                                   // exact.cpp:49-53
     b.lower = b.upper = 0;
@@ -283,7 +417,10 @@ void Solver::exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw
   }
   const size_t budget = (size_t)cfg.max_memory_mb * 1024 * 1024;
   const size_t row_bytes = sizeof(u64) * W;
-  const u64 max_rt = b.upper - 1;  // exact.cpp:65
+  // exact.cpp:65 searches lengths below the upper bound; when no word backs
+  // that bound (it came from the plan's upper_bound), length == bound is
+  // searched too so that a word can be returned.
+  const u64 max_rt = b.has_word ? b.upper - 1 : b.upper;
   u64 rt = 0;
   bool found = false, oom = false;
   u32 wit_q = 0, wit_s = 0;
@@ -341,9 +478,11 @@ void Solver::exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw
     // upper bound, the bound is the answer (its word, if any, came from the
     // algorithm that set it).  Otherwise (memory budget) only a lower bound.
     (void)oom;
-    rt++;
-    b.lower = std::max<u64>(b.lower, rt);
-    if (rt == b.upper) b.upper = rt;
+    if (rt + 1 >= b.upper) {
+      b.lower = std::max<u64>(b.lower, b.upper);
+    } else {
+      b.lower = std::max<u64>(b.lower, rt + 1);
+    }
   }
   st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   E.st = nullptr;
@@ -387,7 +526,9 @@ static BeamRun beam_cutoff(Engine& E, const Automaton& A, u32 beam_size, u64 max
     E.flags_a.reserve(sizeof(u32) * N);
     E.uq_vals.reserve(sizeof(u32) * N);
     E.keys_alt.reserve(sizeof(u64) * R * N);
-    launch_expand(W, false, X.rows.as<u64>(), m, E.tables, E.ch_rows.as<u64>(), E.stream);
+    E.timed(1, (double)m * 8.0 * W * (1 + k), [&] {
+      launch_expand(W, false, X.rows.as<u64>(), m, E.tables, E.ch_rows.as<u64>(), E.stream);
+    });
     launch_beam_keys(W, E.ch_rows.as<u64>(), Nc, n, R, E.keys.as<u64>(), E.stream);
     launch_iota(E.ch_vals.as<u32>(), Nc, E.stream);
     E.count_launch(3);

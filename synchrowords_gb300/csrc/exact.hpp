@@ -41,6 +41,10 @@ class Solver {
   uint64_t sort_unique(uint32_t n, uint64_t* sets, uint64_t count);
 
   int device() const { return device_; }
+  void* stream() const;  // the cudaStream_t every kernel of this solver runs on
+  // Per-kernel-class CUDA-event timing of everything launched in between.
+  void profile_begin();
+  void profile_end(sw_kernel_profile out[4]);
 
  private:
   int device_;

@@ -484,14 +484,14 @@ size_t sort_temp_bytes(int R, u32 m) {
 }
 
 template <int R>
-static void radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
-  if (m <= 1) return;
+static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+  if (m <= 1) return 0;
   if (m <= small_sort_max<R>()) {
     size_t smem = (size_t)m * (2 * R * sizeof(u64) + 2 * sizeof(u32));
     SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m);
     SW_LAUNCH_CHECK();
-    return;
+    return 1;
   }
   const u32 ntiles = (m + kRsTile - 1) / kRsTile;
   char* t = static_cast<char*>(temp);
@@ -511,6 +511,7 @@ static void radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt
   SW_CUDA(cudaStreamSynchronize(s));
   u64 *ki = keys, *ko = keys_alt;
   u32 *vi = vals, *vo = vals_alt;
+  int passes = 0;
   for (int word = R - 1; word >= 0; --word) {
     const u64 vary = h_or[word] ^ h_and[word];
     for (int shift = 0; shift < 64; shift += 8) {
@@ -521,15 +522,17 @@ static void radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt
       SW_LAUNCH_CHECK();
       std::swap(ki, ko);
       std::swap(vi, vo);
+      ++passes;
     }
   }
   if (ki != keys) {
     SW_CUDA(cudaMemcpyAsync(keys, ki, sizeof(u64) * R * (size_t)m, cudaMemcpyDeviceToDevice, s));
     SW_CUDA(cudaMemcpyAsync(vals, vi, sizeof(u32) * (size_t)m, cudaMemcpyDeviceToDevice, s));
   }
+  return 1 + 5 * passes;  // or/and reduction + (upsweep, 3 scan kernels, downsweep) per pass
 }
 
-void radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+int radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
   switch (R) {
     case 1: return radix_sort_rows_t<1>(keys, vals, keys_alt, vals_alt, m, temp, s);
     case 2: return radix_sort_rows_t<2>(keys, vals, keys_alt, vals_alt, m, temp, s);
@@ -603,16 +606,31 @@ __global__ void k_fill_u32(u32* p, u32 v, u32 m) {
     default: throw std::runtime_error("unsupported set width"); \
   }
 
+// Row widths of sort keys: set widths 1/2/4/8 and beam keys (1 + ceil(n/64)).
+#define SW_DISPATCH_R(R, ...)                                 \
+  switch (R) {                                                \
+    case 1: { constexpr int RR = 1; __VA_ARGS__; } break;     \
+    case 2: { constexpr int RR = 2; __VA_ARGS__; } break;     \
+    case 3: { constexpr int RR = 3; __VA_ARGS__; } break;     \
+    case 4: { constexpr int RR = 4; __VA_ARGS__; } break;     \
+    case 5: { constexpr int RR = 5; __VA_ARGS__; } break;     \
+    case 6: { constexpr int RR = 6; __VA_ARGS__; } break;     \
+    case 7: { constexpr int RR = 7; __VA_ARGS__; } break;     \
+    case 8: { constexpr int RR = 8; __VA_ARGS__; } break;     \
+    case 9: { constexpr int RR = 9; __VA_ARGS__; } break;     \
+    default: throw std::runtime_error("unsupported row width"); \
+  }
+
 void launch_unique_flags(int W, const u64* rows, u32 m, u32* flags, cudaStream_t s) {
   if (!m) return;
-  SW_DISPATCH_W(W, (k_unique_flags<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, flags)));
+  SW_DISPATCH_R(W, (k_unique_flags<RR><<<(m + 255) / 256, 256, 0, s>>>(rows, m, flags)));
   SW_LAUNCH_CHECK();
 }
 
 void launch_compact(int W, const u64* rows, const u32* vals, const u32* flags, const u32* pos, u32 m, u64* out_rows,
                     u32* out_vals, cudaStream_t s) {
   if (!m) return;
-  SW_DISPATCH_W(W, (k_compact<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, vals, flags, pos, m, out_rows, out_vals)));
+  SW_DISPATCH_R(W, (k_compact<RR><<<(m + 255) / 256, 256, 0, s>>>(rows, vals, flags, pos, m, out_rows, out_vals)));
   SW_LAUNCH_CHECK();
 }
 
@@ -709,10 +727,12 @@ constexpr int kStack = 40;
 template <int W, int MODE>
 __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u32 m, const u32* __restrict__ gamma,
                                                     const u32* __restrict__ split, const u64* __restrict__ Q, u32 q,
-                                                    int n, u32* __restrict__ flags, u32* witness, int stop) {
+                                                    int n, u32* __restrict__ flags, u32* witness, int stop,
+                                                    u64* __restrict__ bytes_ctr) {
   const u32 qi = blockIdx.x * blockDim.x + threadIdx.x;
   if (qi >= q) return;
-  if (stop && *(volatile u32*)witness) return;
+  u32 rows_read = 1, nodes_read = 0;  // algorithmic traffic: rows of W words, 8-byte node records
+  bool quit = stop && *(volatile u32*)witness;
   u64 c[W];
 #pragma unroll
   for (int w = 0; w < W; ++w) {
@@ -721,6 +741,7 @@ __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u
   }
   auto test = [&](u32 idx) -> bool {
     const u64* s = S + (size_t)idx * W;
+    ++rows_read;
     bool eq = true;
 #pragma unroll
     for (int w = 0; w < W; ++w) {
@@ -740,7 +761,7 @@ __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u
         return;
       }
   };
-  if (m == 0) {
+  if (m == 0 || quit) {
   } else if (m <= (u32)kLeaf) {
     scan(0, m - 1);
   } else {
@@ -758,8 +779,13 @@ __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u
         scan(lo, hi);
         continue;
       }
-      if (stop && ((++iter & 31) == 0) && *(volatile u32*)witness) return;
+      if (stop && ((++iter & 31) == 0) && *(volatile u32*)witness) {
+        quit = true;
+        break;
+      }
       const u32 g = gamma[x], b = split[x];
+      nodes_read += 1;
+      rows_read += 1;
       // (a) common prefix bits [0, b) of the range must lie inside c
       bool ok = true;
       const u64* s = S + (size_t)lo * W;
@@ -799,7 +825,12 @@ __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u
       }
     }
   }
-  if (!hit) return;
+  if (bytes_ctr) {
+    const u32 mask = __activemask();
+    const u32 r = __reduce_add_sync(mask, rows_read), nd = __reduce_add_sync(mask, nodes_read);
+    if ((threadIdx.x & 31) == (u32)(__ffs(mask) - 1)) atomicAdd(bytes_ctr, (u64)r * (8 * W) + (u64)nd * 8);
+  }
+  if (!hit || quit) return;
   if (stop) {
     if (atomicCAS(witness, 0u, 1u) == 0u) {
       witness[1] = qi;
@@ -811,19 +842,19 @@ __global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u
 }
 
 void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q, u32 q,
-                       int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s) {
+                       int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s, u64* bytes_ctr) {
   if (!q || !m) return;
   const u32 blocks = (q + 127) / 128;
 #define SW_Q(WW)                                                                                                  \
   case WW:                                                                                                        \
     if (mode == kQuerySubset)                                                                                     \
-      k_trie_query<WW, kQuerySubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness, stop_at_first); \
+      k_trie_query<WW, kQuerySubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness, stop_at_first, bytes_ctr); \
     else if (mode == kQueryProperSubset)                                                                          \
       k_trie_query<WW, kQueryProperSubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,   \
-                                                                  stop_at_first);                                 \
+                                                                  stop_at_first, bytes_ctr);                      \
     else                                                                                                          \
       k_trie_query<WW, kQueryDisjoint><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,       \
-                                                              stop_at_first);                                     \
+                                                              stop_at_first, bytes_ctr);                          \
     break;
   switch (W) {
     SW_Q(1)

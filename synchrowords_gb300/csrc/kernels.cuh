@@ -39,9 +39,9 @@ void launch_scan(const u32* in, u32* out, u32 n, u32* total_dev, void* temp, cud
 
 // Stable LSD radix sort of m rows of R words (word 0 most significant) with
 // a u32 payload.  Result lands in (keys, vals); (keys_alt, vals_alt) are
-// scratch of the same size.  `bitmask_dev` (R words) must hold the OR^AND of
-// all rows if `have_mask`, else it is computed here.
-void radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp,
+// scratch of the same size.  Digits constant over all rows are skipped.
+// Returns the number of kernels launched.
+int radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp,
                      cudaStream_t s);
 
 // flags[i] = 1 if row i differs from row i-1 (rows sorted).
@@ -65,8 +65,20 @@ enum QueryMode : int {
 // Trie query: for each query row c, flags[c] |= hit(c) (or, with
 // `stop_at_first`, record one witness pair and let all threads exit early).
 // witness[0] = found flag, witness[1] = query index, witness[2] = set index.
+// `bytes_ctr` (optional) accumulates the algorithmic bytes the walk reads:
+// 8*W per row compared (query, prefix and leaf rows) + 8 per tree node.
 void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q,
-                       u32 q, int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s);
+                       u32 q, int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s,
+                       u64* bytes_ctr = nullptr);
+
+// Tiled subset check (subset_check.cu), same semantics as launch_trie_query:
+// S sorted, cut into 64-row tiles; tile_and[t] (W words) = AND of the tile's
+// rows, from launch_tile_and.  `flags` must start zeroed (non-stop mode).
+// `bytes_ctr` (optional) accumulates the bytes of S tiles staged on chip.
+size_t subset_check_temp_bytes(int W, u32 m);
+void launch_tile_and(int W, const u64* S, u32 m, u64* tile_and, cudaStream_t s);
+void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* tile_and, const u64* Q, u32 q, int n,
+                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr = nullptr);
 
 // out = sorted merge of two sorted, mutually disjoint row arrays.
 void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);

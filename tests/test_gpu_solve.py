@@ -130,3 +130,14 @@ def test_non_synchronizing(ctx):
 def test_single_state(ctx):
     r = ctx.solve([0, 0, 0, 0], 1, 4, EXACT)
     assert (r.lower, r.upper) == (0, 0)
+
+
+def test_solve_batch_concurrent_streams(ctx):
+    autos = [(48, 2, random_dfa(48, 2, 900 + i)) for i in range(12)] + \
+            [(100, 3, random_dfa(100, 3, 950 + i)) for i in range(4)] + [(28, 2, cerny(28))]
+    res = ctx.solve_batch(autos, EXACT, workers=6)
+    assert len(res) == len(autos)
+    for (n, k, d), r in zip(autos, res):
+        ref = oracle.exact(d, n, k)
+        assert (r.lower, r.upper) == (ref.lower, ref.upper)
+        check_word(d, n, k, r)
