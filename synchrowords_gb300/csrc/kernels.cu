@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "kernels.cuh"
@@ -488,7 +489,13 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
   if (m <= 1) return 0;
   if (m <= small_sort_max<R>()) {
     size_t smem = (size_t)m * (2 * R * sizeof(u64) + 2 * sizeof(u32));
-    SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    // Raise the opt-in once, to the largest size this path uses: lowering it
+    // per call would race with launches of other host threads.
+    static std::once_flag once;
+    std::call_once(once, [] {
+      const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
+      SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+    });
     k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m);
     SW_LAUNCH_CHECK();
     return 1;
