@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <stdexcept>
@@ -236,6 +238,14 @@ class Engine {
     }
   }
 
+  // Step log on stderr when SYNCHRO_VERBOSE is set (synchronises per phase).
+  const bool verbose = std::getenv("SYNCHRO_VERBOSE") != nullptr;
+  double vclock() {
+    if (!verbose) return 0.0;
+    SW_CUDA(cudaStreamSynchronize(stream));
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
+
   // One BFS layer on side X (forward = image, backward = preimage of complements).
   void step(Side& X, bool forward, int W, int n, int k) {
     const u32 m = X.count;
@@ -249,6 +259,7 @@ class Engine {
     flags_a.reserve(sizeof(u32) * N);
     flags_b.reserve(sizeof(u32) * N);
     keep.reserve(sizeof(u32) * N);
+    const double t_step0 = vclock();
     // expansion reads each parent row and writes k child rows
     timed(1, (double)m * 8.0 * W * (1 + k), [&] {
       launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream);
@@ -265,12 +276,30 @@ class Engine {
     launch_fill_u32(flags_a.as<u32>(), 0, u, stream);
     launch_fill_u32(flags_b.as<u32>(), 0, u, stream);
     count_launch(2);
+    const double t_sort = vclock();
     if (X.vis_count)
       query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split, uq_rows.as<u64>(), u, n,
             flags_a.as<u32>(), false);
+    const double t_vis = vclock();
     build_tree(W, uq_rows.as<u64>(), u, tmp_gamma, tmp_split);
     query(W, kQueryProperSubset, uq_rows.as<u64>(), u, tmp_gamma, tmp_split, uq_rows.as<u64>(), u, n,
           flags_b.as<u32>(), false);
+    const double t_self = vclock();
+    if (verbose) {
+      std::vector<u32> fa(u), fb(u);
+      SW_CUDA(cudaMemcpy(fa.data(), flags_a.p, sizeof(u32) * u, cudaMemcpyDeviceToHost));
+      SW_CUDA(cudaMemcpy(fb.data(), flags_b.p, sizeof(u32) * u, cudaMemcpyDeviceToHost));
+      size_t cv = 0, cs = 0;
+      for (u32 i = 0; i < u; ++i) {
+        cv += fa[i] != 0;
+        cs += fb[i] != 0;
+      }
+      std::fprintf(stderr,
+                   "[sw] %s parents=%u children=%u unique=%u visited=%u dropped_by_visited=%zu dropped_by_self=%zu "
+                   "| expand+sort+unique %.3f ms, visited check %.3f ms, self check %.3f ms\n",
+                   forward ? "BFS " : "IBFS", m, Nc, u, X.vis_count, cv, cs, t_sort - t_step0, t_vis - t_sort,
+                   t_self - t_vis);
+    }
     launch_keep_flags(flags_a.as<u32>(), flags_b.as<u32>(), u, keep.as<u32>(), stream);
     count_launch();
     X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(u, 1));
@@ -442,6 +471,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       st.ibfs_steps++;
     }
     // meet check: some F disjoint from some B-complement (F ⊆ B)
+    const double t_meet0 = E.vclock();
     SW_CUDA(cudaMemsetAsync(E.d_misc, 0, 4 * sizeof(u32), E.stream));
     E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split, E.B.rows.as<u64>(), E.B.count,
             n, nullptr, true);
@@ -449,6 +479,9 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
     SW_CUDA(cudaStreamSynchronize(E.stream));
     const u32* w = E.pinned.as<u32>();
+    if (E.verbose)
+      std::fprintf(stderr, "[sw] len %llu: |F|=%u |B|=%u meet check %.3f ms%s\n", (unsigned long long)rt, E.F.count,
+                   E.B.count, E.vclock() - t_meet0, w[0] ? " -> found" : "");
     if (w[0]) {
       found = true;
       wit_q = w[1];

@@ -6,58 +6,33 @@
 // kernel cuda/subsets_implicit_trie_kernel.cu:13-92).  The trie's pruning is
 // re-expressed as a prefix-partitioned candidate filter:
 //   * S is sorted (lexicographically, most frequent states first) and cut into
-//     leaf tiles of 32 consecutive rows;
-//   * an implicit binary tree over the tiles stores, per node, the AND of all
-//     rows below it — the states every set of that range contains.  For sorted
-//     rows this is the range's common prefix (the trie node's path) plus
-//     incidental shared states;
-//   * a query that lacks one of a node's states cannot contain any set below
-//     it.
-// One warp owns 32 consecutive (hence similar) queries and walks the tree
-// depth-first; it descends into a node only if some lane still needs it
-// (__any_sync), so the walk is warp-uniform.  A needed leaf tile is loaded
-// with one coalesced read (lane r holds row r) and broadcast row by row with
-// shuffles; every lane tests its own query with an early exit on word 0.
-// Warps stop as soon as all their queries are decided; in meet mode the
-// first hit of any warp stops the grid.
+//     tiles of 64 consecutive rows, grouped 16 to a super-tile;
+//   * every tile and super-tile keeps the AND of its rows — the states all of
+//     its sets contain.  For sorted rows that is the range's common prefix
+//     (the trie node's path) plus incidental shared states;
+//   * a query that lacks one of those states cannot contain any set of the
+//     range.
+// One warp owns 32 consecutive (hence similar) queries and streams the
+// super-tiles of its chunk of S: a range is skipped unless some lane still
+// needs it (__any_sync), a needed tile is staged into the warp's slice of
+// shared memory with one coalesced read, and every lane tests its own query
+// against the staged rows with an early exit on word 0.  No block-wide
+// barriers: warps of a block proceed independently.  Warps stop as soon as all
+// their queries are decided; in meet mode the first hit stops the grid.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <vector>
 
 #include "kernels.cuh"
 
 namespace sw {
 
 namespace {
-constexpr int kLeafRows = 32;
-constexpr int kWarps = 4;
-constexpr int kMaxLevels = 32;
-constexpr int kStackPerWarp = 2 * kMaxLevels + 2;
+constexpr int kTileRows = 64;
+constexpr int kTilesPerSuper = 16;
+constexpr int kSuperRows = kTileRows * kTilesPerSuper;
+constexpr int kWarps = 8;
 constexpr u32 kFullMask = 0xffffffffu;
-
-struct TreeShape {
-  int levels;                // level 0 = leaves
-  u32 count[kMaxLevels];     // nodes per level
-  u32 offset[kMaxLevels];    // first node of the level in the node array
-};
-
-TreeShape tree_shape(u32 m) {
-  TreeShape t{};
-  u32 c = (m + kLeafRows - 1) / kLeafRows;
-  u32 off = 0;
-  int l = 0;
-  while (true) {
-    t.count[l] = c;
-    t.offset[l] = off;
-    off += c;
-    ++l;
-    if (c <= 1) break;
-    c = (c + 1) / 2;
-  }
-  t.levels = l;
-  return t;
-}
 
 int sm_count_sc() {
   static int cached = 0;
@@ -68,44 +43,38 @@ int sm_count_sc() {
   }
   return cached;
 }
+
+__host__ __device__ inline u32 n_tiles(u32 m) { return (m + kTileRows - 1) / kTileRows; }
+__host__ __device__ inline u32 n_supers(u32 m) { return (m + kSuperRows - 1) / kSuperRows; }
 }  // namespace
 
-// Level 0: AND of each 32-row leaf tile.
+// AND masks: tiles first (n_tiles(m) entries), then super-tiles.
 template <int W>
-__global__ void k_leaf_and(const u64* __restrict__ S, u32 m, u64* __restrict__ nodes) {
-  const u32 leaves = (m + kLeafRows - 1) / kLeafRows;
+__global__ void k_range_and(const u64* __restrict__ S, u32 m, u64* __restrict__ masks) {
+  const u32 tiles = n_tiles(m), supers = n_supers(m);
   const u32 id = blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= leaves * W) return;
-  const u32 t = id / W, w = id % W;
-  const u32 r0 = t * kLeafRows, r1 = min(m, r0 + kLeafRows);
+  if (id >= (tiles + supers) * W) return;
+  const u32 node = id / W, w = id % W;
+  u32 r0, r1;
+  if (node < tiles) {
+    r0 = node * kTileRows;
+    r1 = min(m, r0 + kTileRows);
+  } else {
+    r0 = (node - tiles) * kSuperRows;
+    r1 = min(m, r0 + kSuperRows);
+  }
   u64 a = ~0ULL;
   for (u32 r = r0; r < r1; ++r) a &= S[(size_t)r * W + w];
-  nodes[id] = a;
-}
-
-// Upper levels, one block, level by level.
-template <int W>
-__global__ void __launch_bounds__(1024) k_upper_and(u64* nodes, TreeShape t) {
-  for (int l = 1; l < t.levels; ++l) {
-    const u32 cnt = t.count[l], prev = t.count[l - 1];
-    for (u32 id = threadIdx.x; id < cnt * W; id += blockDim.x) {
-      const u32 i = id / W, w = id % W;
-      const u32 c0 = 2 * i, c1 = 2 * i + 1;
-      u64 a = nodes[((size_t)t.offset[l - 1] + c0) * W + w];
-      if (c1 < prev) a &= nodes[((size_t)t.offset[l - 1] + c1) * W + w];
-      nodes[((size_t)t.offset[l] + i) * W + w] = a;
-    }
-    __syncthreads();
-  }
+  masks[id] = a;
 }
 
 template <int W, int MODE>
-__global__ void __launch_bounds__(kWarps * 32) k_subset_tree(const u64* __restrict__ S, u32 m,
-                                                             const u64* __restrict__ nodes, TreeShape t,
-                                                             int start_level, const u64* __restrict__ Q, u32 q,
-                                                             int n, u32* __restrict__ flags, u32* witness, int stop,
+__global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restrict__ S, u32 m,
+                                                             const u64* __restrict__ masks, u32 supers_per_chunk,
+                                                             const u64* __restrict__ Q, u32 q, int n,
+                                                             u32* __restrict__ flags, u32* witness, int stop,
                                                              u64* __restrict__ bytes_ctr) {
-  __shared__ u32 s_stack[kWarps][kStackPerWarp];
+  __shared__ __align__(16) u64 s_rows[kWarps][kTileRows * W];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const u32 qi = (blockIdx.x * kWarps + warp) * 32 + lane;
   const bool valid = qi < q;
@@ -119,46 +88,41 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_tree(const u64* __restri
   bool hit = false;
   u32 hit_idx = 0;
   u64 loaded = 0;
-  u32* st = s_stack[warp];
-  int sp = 0;
-  // this warp's subtree root: node blockIdx.y of level start_level
-  if (blockIdx.y < t.count[start_level]) {
-    if (lane == 0) st[0] = ((u32)start_level << 26) | blockIdx.y;
-    sp = 1;
-  }
-  __syncwarp();
-  int iter = 0;
-  while (sp > 0) {
+  const u32 tiles = n_tiles(m), supers = n_supers(m);
+  const u64* tile_and = masks;
+  const u64* super_and = masks + (size_t)tiles * W;
+  u64* my_rows = s_rows[warp];
+  const u32 s0 = blockIdx.y * supers_per_chunk;
+  const u32 s1 = min(supers, s0 + supers_per_chunk);
+  for (u32 sp = s0; sp < s1; ++sp) {
     if (__all_sync(kFullMask, done)) break;
-    if (stop && ((++iter & 7) == 0)) {
+    if (stop) {
       u32 f = lane == 0 ? *(volatile u32*)witness : 0u;
       if (__shfl_sync(kFullMask, f, 0)) break;
     }
-    --sp;
-    const u32 e = st[sp];
-    __syncwarp();
-    const int l = (int)(e >> 26);
-    const u32 i = e & ((1u << 26) - 1);
-    const u64* nd = nodes + ((size_t)t.offset[l] + i) * W;
-    bool need = !done;
+    bool need_s = !done;
 #pragma unroll
     for (int w = 0; w < W; ++w)
-      if (nd[w] & ~c[w]) need = false;
-    if (!__any_sync(kFullMask, need)) continue;
-    if (l == 0) {
-      const u32 r0 = i * kLeafRows;
-      const u32 rows = min((u32)kLeafRows, m - r0);
-      u64 my[W];
+      if (super_and[(size_t)sp * W + w] & ~c[w]) need_s = false;
+    if (!__any_sync(kFullMask, need_s)) continue;
+    const u32 t1 = min(tiles, (sp + 1) * kTilesPerSuper);
+    for (u32 t = sp * kTilesPerSuper; t < t1; ++t) {
+      bool need = need_s && !done;
 #pragma unroll
-      for (int w = 0; w < W; ++w) my[w] = (lane < (int)rows) ? S[((size_t)r0 + lane) * W + w] : ~0ULL;
+      for (int w = 0; w < W; ++w)
+        if (tile_and[(size_t)t * W + w] & ~c[w]) need = false;
+      if (!__any_sync(kFullMask, need)) continue;
+      const u32 r0 = t * kTileRows;
+      const u32 rows = min((u32)kTileRows, m - r0);
+      const u64* src = S + (size_t)r0 * W;
+      for (u32 i = lane; i < rows * W; i += 32) my_rows[i] = src[i];
       loaded += rows;
-      for (u32 r = 0; r < rows; ++r) {
-        u64 s[W];
-#pragma unroll
-        for (int w = 0; w < W; ++w) s[w] = __shfl_sync(kFullMask, my[w], r);
-        if (need && !done) {
-          bool sub = !(s[0] & ~c[0]);
-          bool eq = (s[0] == c[0]);
+      __syncwarp();
+      if (need) {
+        for (u32 r = 0; r < rows; ++r) {
+          const u64* s = my_rows + r * W;
+          if (s[0] & ~c[0]) continue;
+          bool sub = true, eq = (s[0] == c[0]);
 #pragma unroll
           for (int w = 1; w < W; ++w) {
             sub = sub && !(s[w] & ~c[w]);
@@ -168,9 +132,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_tree(const u64* __restri
             hit = true;
             done = true;
             hit_idx = r0 + r;
+            break;
           }
         }
       }
+      __syncwarp();
       if (stop && hit) {
         if (atomicCAS(witness, 0u, 1u) == 0u) {
           witness[1] = qi;
@@ -178,15 +144,6 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_tree(const u64* __restri
         }
         hit = false;  // recorded
       }
-    } else {
-      const u32 c0 = 2 * i, c1 = 2 * i + 1;
-      if (lane == 0) {
-        if (c1 < t.count[l - 1]) st[sp++] = ((u32)(l - 1) << 26) | c1;
-        st[sp++] = ((u32)(l - 1) << 26) | c0;
-      } else {
-        sp += (c1 < t.count[l - 1]) ? 2 : 1;
-      }
-      __syncwarp();
     }
   }
   if (bytes_ctr && lane == 0 && loaded) atomicAdd(bytes_ctr, loaded * 8ULL * W);
@@ -194,54 +151,45 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_tree(const u64* __restri
 }
 
 size_t subset_check_temp_bytes(int W, u32 m) {
-  TreeShape t = tree_shape(std::max<u32>(m, 1));
-  u32 total = t.offset[t.levels - 1] + t.count[t.levels - 1];
-  return sizeof(u64) * (size_t)W * (total + 1);
+  return sizeof(u64) * (size_t)W * (n_tiles(std::max<u32>(m, 1)) + n_supers(std::max<u32>(m, 1)) + 1);
 }
 
-void launch_tile_and(int W, const u64* S, u32 m, u64* nodes, cudaStream_t s) {
+void launch_tile_and(int W, const u64* S, u32 m, u64* masks, cudaStream_t s) {
   if (!m) return;
-  TreeShape t = tree_shape(m);
-  const u32 threads = t.count[0] * W;
+  const u32 threads = (n_tiles(m) + n_supers(m)) * W;
   switch (W) {
-    case 1: k_leaf_and<1><<<(threads + 255) / 256, 256, 0, s>>>(S, m, nodes); break;
-    case 2: k_leaf_and<2><<<(threads + 255) / 256, 256, 0, s>>>(S, m, nodes); break;
-    case 4: k_leaf_and<4><<<(threads + 255) / 256, 256, 0, s>>>(S, m, nodes); break;
-    case 8: k_leaf_and<8><<<(threads + 255) / 256, 256, 0, s>>>(S, m, nodes); break;
-    default: throw std::runtime_error("tile_and: unsupported width");
-  }
-  if (t.levels > 1) {
-    switch (W) {
-      case 1: k_upper_and<1><<<1, 1024, 0, s>>>(nodes, t); break;
-      case 2: k_upper_and<2><<<1, 1024, 0, s>>>(nodes, t); break;
-      case 4: k_upper_and<4><<<1, 1024, 0, s>>>(nodes, t); break;
-      case 8: k_upper_and<8><<<1, 1024, 0, s>>>(nodes, t); break;
-    }
+    case 1: k_range_and<1><<<(threads + 255) / 256, 256, 0, s>>>(S, m, masks); break;
+    case 2: k_range_and<2><<<(threads + 255) / 256, 256, 0, s>>>(S, m, masks); break;
+    case 4: k_range_and<4><<<(threads + 255) / 256, 256, 0, s>>>(S, m, masks); break;
+    case 8: k_range_and<8><<<(threads + 255) / 256, 256, 0, s>>>(S, m, masks); break;
+    default: throw std::runtime_error("range_and: unsupported width");
   }
   SW_LAUNCH_CHECK();
 }
 
-void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* nodes, const u64* Q, u32 q, int n,
+void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks, const u64* Q, u32 q, int n,
                          u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr) {
   if (!m || !q) return;
-  TreeShape t = tree_shape(m);
+  const u32 supers = n_supers(m);
   const u32 qblocks = (q + kWarps * 32 - 1) / (kWarps * 32);
-  // start the walks below the root so that (query blocks x subtrees) covers the GPU ~4x
+  // split S into chunks of super-tiles so that the grid covers the GPU ~4x
   const u32 target = (u32)sm_count_sc() * 4;
-  int start = t.levels - 1;
-  while (start > 0 && qblocks * t.count[start] < target && t.count[start - 1] <= 65535) --start;
-  dim3 grid(qblocks, t.count[start]);
-#define SW_SC(WW)                                                                                                 \
-  case WW:                                                                                                        \
-    if (mode == kQuerySubset)                                                                                     \
-      k_subset_tree<WW, kQuerySubset><<<grid, kWarps * 32, 0, s>>>(S, m, nodes, t, start, Q, q, n, flags,       \
-                                                                   witness, stop, bytes_ctr);                     \
-    else if (mode == kQueryProperSubset)                                                                          \
-      k_subset_tree<WW, kQueryProperSubset><<<grid, kWarps * 32, 0, s>>>(S, m, nodes, t, start, Q, q, n, flags, \
-                                                                         witness, stop, bytes_ctr);               \
-    else                                                                                                          \
-      k_subset_tree<WW, kQueryDisjoint><<<grid, kWarps * 32, 0, s>>>(S, m, nodes, t, start, Q, q, n, flags,     \
-                                                                     witness, stop, bytes_ctr);                   \
+  u32 chunks = std::max<u32>(1, std::min<u32>(supers, (target + qblocks - 1) / qblocks));
+  chunks = std::min<u32>(chunks, 65535);
+  const u32 per = (supers + chunks - 1) / chunks;
+  chunks = (supers + per - 1) / per;
+  dim3 grid(qblocks, chunks);
+#define SW_SC(WW)                                                                                              \
+  case WW:                                                                                                     \
+    if (mode == kQuerySubset)                                                                                  \
+      k_subset_scan<WW, kQuerySubset><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags, witness, \
+                                                                   stop, bytes_ctr);                           \
+    else if (mode == kQueryProperSubset)                                                                       \
+      k_subset_scan<WW, kQueryProperSubset><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags,    \
+                                                                         witness, stop, bytes_ctr);            \
+    else                                                                                                       \
+      k_subset_scan<WW, kQueryDisjoint><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags,        \
+                                                                     witness, stop, bytes_ctr);                \
     break;
   switch (W) {
     SW_SC(1)
