@@ -115,24 +115,44 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
       const u32 r0 = t * kTileRows;
       const u32 rows = min((u32)kTileRows, m - r0);
       const u64* src = S + (size_t)r0 * W;
-      for (u32 i = lane; i < rows * W; i += 32) my_rows[i] = src[i];
+      if (W >= 2) {
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(my_rows);
+        for (u32 i = lane; i < rows * W / 2; i += 32) d4[i] = s4[i];
+      } else {
+        for (u32 i = lane; i < rows; i += 32) my_rows[i] = src[i];
+      }
+      // rows past the end of S never pass the word-0 test below
+      if (rows < (u32)kTileRows)
+        for (u32 i = rows * W + lane; i < (u32)kTileRows * W; i += 32) my_rows[i] = ~0ULL;
       loaded += rows;
       __syncwarp();
       if (need) {
-        for (u32 r = 0; r < rows; ++r) {
-          const u64* s = my_rows + r * W;
-          if (s[0] & ~c[0]) continue;
-          bool sub = true, eq = (s[0] == c[0]);
+        const u64 nc0 = ~c[0];
+        // four rows per iteration: independent word-0 tests, full test only
+        // for the (rare) rows that pass
+        for (u32 r = 0; r < (u32)kTileRows && !done; r += 4) {
+          const u64 a0 = my_rows[(r + 0) * W], a1 = my_rows[(r + 1) * W];
+          const u64 a2 = my_rows[(r + 2) * W], a3 = my_rows[(r + 3) * W];
+          const unsigned pass = (!(a0 & nc0) ? 1u : 0u) | (!(a1 & nc0) ? 2u : 0u) | (!(a2 & nc0) ? 4u : 0u) |
+                                (!(a3 & nc0) ? 8u : 0u);
+          if (!pass) continue;
 #pragma unroll
-          for (int w = 1; w < W; ++w) {
-            sub = sub && !(s[w] & ~c[w]);
-            eq = eq && (s[w] == c[w]);
-          }
-          if (sub && (MODE != kQueryProperSubset || !eq)) {
-            hit = true;
-            done = true;
-            hit_idx = r0 + r;
-            break;
+          for (int j = 0; j < 4; ++j) {
+            if (!((pass >> j) & 1u) || r + j >= rows) continue;
+            const u64* s = my_rows + (r + j) * W;
+            bool sub = true, eq = (s[0] == c[0]);
+#pragma unroll
+            for (int w = 1; w < W; ++w) {
+              sub = sub && !(s[w] & ~c[w]);
+              eq = eq && (s[w] == c[w]);
+            }
+            if (sub && (MODE != kQueryProperSubset || !eq)) {
+              hit = true;
+              done = true;
+              hit_idx = r0 + r + j;
+              break;
+            }
           }
         }
       }
@@ -172,8 +192,10 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
   if (!m || !q) return;
   const u32 supers = n_supers(m);
   const u32 qblocks = (q + kWarps * 32 - 1) / (kWarps * 32);
-  // split S into chunks of super-tiles so that the grid covers the GPU ~4x
-  const u32 target = (u32)sm_count_sc() * 4;
+  // split S into chunks of super-tiles so that the grid covers the GPU ~16x:
+  // per-warp work varies a lot (early exits, filter hit rates), and many small
+  // blocks keep the SMs busy until the slowest ones finish
+  const u32 target = (u32)sm_count_sc() * 16;
   u32 chunks = std::max<u32>(1, std::min<u32>(supers, (target + qblocks - 1) / qblocks));
   chunks = std::min<u32>(chunks, 65535);
   const u32 per = (supers + chunks - 1) / chunks;
