@@ -1,0 +1,187 @@
+"""Host-side tests (no GPU): the C ABI library loads and exports every
+declared entry point, config expressions evaluate with C++ semantics (checked
+against g++ itself), plans parse like the reference's config classes, the CLI
+parses the reference's flags, and the bench contract's CPU pieces work."""
+import ctypes
+import json
+import os
+import re
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+import synchrowords_gb300 as sw
+
+ROOT = Path(__file__).resolve().parents[1]
+HEADER = ROOT / "include" / "synchrowords.h"
+
+
+def declared_symbols():
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*|void\*)\s+\**(sw_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    names = declared_symbols()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(native_lib, name), f"{name} missing from the shared library"
+
+
+def test_version_and_no_device_error(native_lib):
+    assert b"sm_103a" in native_lib.sw_version()
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(sw.SynchroError) as e:
+        sw.Context(0)
+    assert e.value.code == -4  # SW_ERR_NO_DEVICE: no silent CPU path
+
+
+EXPRESSIONS = [
+    "AUT_N * 16", "AUT_N * std::log2(AUT_N)", "AUT_N * AUT_N * std::log2(AUT_N)", "1ULL * AUT_N * AUT_N * AUT_N / 6",
+    "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1", "12 * 1024", "1024 * 2", "AUT_N * AUT_K", "AUT_N * AUT_K * AUT_K * 8",
+    "std::log2(AUT_N)", "std::sqrt(AUT_N) * 3", "std::pow(AUT_K, 10)", "AUT_N / 3", "-AUT_N / 3", "AUT_N % 7",
+    "(AUT_N < 1000 * 1000)", "AUT_N > 100 ? 10000 : 5000", "AUT_N * AUT_N * AUT_N * AUT_N", "-1", "8192",
+    "static_cast<int>(AUT_N * 1.5)", "(unsigned)AUT_N - 1000", "1U - 2", "AUT_N << 4", "std::floor(AUT_N / 7.0)",
+    "2147483647 + 1", "0.01", "AUT_N * 0.01 + std::exp(1)", "std::min(AUT_N, 64)", "std::max(AUT_K * 5, 3)",
+]
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not available")
+@pytest.mark.parametrize("n,k", [(200, 2), (48, 3), (1, 1), (512, 16), (100000, 7)])
+def test_expression_evaluator_matches_gxx(native_lib, tmp_path, n, k):
+    # The reference compiles plan values as #defines; compile them here too and
+    # compare with the library's evaluator (as uint64 and as double).
+    src = ["#include <cmath>\n#include <cstdio>\n#include <cstdint>\n#include <algorithm>\n",
+           f"#define AUT_N ({n})\n#define AUT_K ({k})\nint main() {{\n"]
+    for e in EXPRESSIONS:
+        src.append(f'  {{ auto v = ({e}); std::printf("%llu %.17g\\n", (unsigned long long)(uint64_t)v, (double)v); }}\n')
+    src.append("  return 0;\n}\n")
+    (tmp_path / "e.cpp").write_text("".join(src))
+    subprocess.run(["g++", "-std=c++17", "-w", "-fwrapv", str(tmp_path / "e.cpp"), "-o", str(tmp_path / "e")],
+                   check=True)
+    out = subprocess.run([str(tmp_path / "e")], capture_output=True, text=True, check=True).stdout.split("\n")
+    for e, line in zip(EXPRESSIONS, out):
+        want_u, want_d = line.split()
+        got_u, got_d = sw.eval_expression(e, n, k)
+        assert float(want_d) == pytest.approx(got_d, rel=1e-15, abs=0), e
+        # uint64 conversion of negative doubles is implementation-defined; skip those
+        if not (float(want_d) < 0 and "." in want_d):
+            assert int(want_u) == got_u, e
+
+
+def test_expression_errors():
+    with pytest.raises(sw.SynchroError):
+        sw.eval_expression("AUT_X * 2", 10, 2)
+    with pytest.raises(sw.SynchroError):
+        sw.eval_expression("(1 + ", 10, 2)
+
+
+# configs/exact.json of the reference (the plan the C5 numbers are quoted on)
+EXACT_JSON = {
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1", "threads": 1, "gpu": False,
+    "algorithms": [
+        {"name": "Brute", "config": {"max_n": "15"}},
+        {"name": "Eppstein", "config": {"transition_tables": False, "find_word": False}},
+        {"name": "Beam", "config": {"presort": "indeg", "dynamic": True, "min_beam_size": "AUT_N * std::log2(AUT_N)",
+                                    "max_beam_size": "AUT_N * AUT_N * std::log2(AUT_N)",
+                                    "beam_exact_ratio": 0.01}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]}
+
+
+def test_plan_evaluation_matches_reference_defines(native_lib):
+    p = sw.plan_from_json(json.dumps(EXACT_JSON), 320, 2)
+    assert p["upper_bound"] == 319 * 319 + 1
+    beam = p["algorithms"][2]
+    # values the reference logs for n = 320 ("min beamsize 2663 max beamsize 852165")
+    assert (beam["min_beam_size"], beam["max_beam_size"]) == (2663, 852165)
+    assert beam["presort_indeg"] == 1 and beam["dynamic"] == 1
+    assert beam["beam_exact_ratio"] == pytest.approx(0.01)
+    ex = p["algorithms"][3]
+    assert (ex["max_memory_mb"], ex["dfs_min_list_size"], ex["bfs_small_list_size"]) == (12288, 8192, 640)
+    d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "Exact", "config": {}}]}), 200, 2)
+    assert d["upper_bound"] == 200 ** 3 // 6
+    ex = d["algorithms"][0]
+    assert (ex["dfs"], ex["dfs_shortcut"], ex["strict_memory_limit"]) == (1, 1, 0)
+    assert (ex["max_memory_mb"], ex["dfs_min_list_size"], ex["bfs_small_list_size"]) == (2048, 10000, 3200)
+
+
+@pytest.mark.parametrize("bad", [
+    '{"algorithms": []}', '{"algorithms": [{"name": "Nope", "config": {}}]}', '{"threads": 0, "algorithms": '
+    '[{"name": "Exact", "config": {}}]}', '{"threads": 65, "algorithms": [{"name": "Exact"}]}',
+    '{"algorithms": [{"name": "Beam", "config": {"presort": "outdeg"}}]}', '{"algorithms": [', 'null'])
+def test_plan_errors(native_lib, bad):
+    with pytest.raises(sw.SynchroError) as e:
+        sw.plan_from_json(bad, 10, 2)
+    assert e.value.code == -2
+
+
+def test_read_automata_and_format(tmp_path):
+    p = tmp_path / "a.txt"
+    p.write_text("2 3\n1 2 0 0 2 2\n4 1\n0 0 0 0\n")
+    autos = sw.read_automata(p)
+    assert autos == [(3, 2, [1, 2, 0, 0, 2, 2]), (1, 4, [0, 0, 0, 0])]
+    r = sw.Result(False, 3, 3, [1, 0, 1], [("Exact", 5)])
+    assert sw.format_result(7, r) == "7: [3, 3] ((Exact, 5)) {1 0 1}"
+    assert sw.format_result(1, sw.Result(True, 0, 0, None, [])) == "1: NON SYNCHRO"
+    (tmp_path / "bad.txt").write_text("2 3\n1 2 0 0 2 9\n")
+    with pytest.raises(ValueError):
+        sw.read_automata(tmp_path / "bad.txt")
+
+
+def test_cli_flags(native_lib, tmp_path):
+    cli = ROOT / "synchrowords_gb300" / "_build" / "synchro"
+    r = subprocess.run([str(cli), "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--continue" in r.stdout
+    r = subprocess.run([str(cli), "-c", "x.json"], capture_output=True, text=True)
+    assert r.returncode == 1  # missing -f (app/args.hpp:42-47)
+    r = subprocess.run([str(cli), "-f", "a", "-c", "b", "-v", "-q"], capture_output=True, text=True)
+    assert r.returncode == 1
+    r = subprocess.run([str(cli), "-f", "a", "-c", "b", "--continue"], capture_output=True, text=True)
+    assert r.returncode == 1
+
+
+def test_bench_reference_arm_runs_on_cpu():
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup",
+                        "0", "--workload", "n48", "--ref-sample", "2"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "ms" and line["higher_is_better"] is False
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def _gloo_worker(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world))
+    import torch.distributed as dist
+    sys.path.insert(0, str(ROOT))
+    import bench
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    v = bench.barrier_max(10.0 * (rank + 1), world)
+    dfas = bench.workload_dfas("n48", rank)
+    dist.destroy_process_group()
+    q.put((rank, v, dfas[0][2][:8]))
+
+
+def test_multi_rank_max_and_disjoint_shards():
+    import multiprocessing as mp
+    import random
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = random.randint(20000, 40000)
+    procs = [ctx.Process(target=_gloo_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    assert [v for _, v, _ in out] == [20.0, 20.0]  # max over ranks
+    assert out[0][2] != out[1][2]  # each rank solves its own automata (weak scaling)
