@@ -140,7 +140,21 @@ class Engine {
   TransTables tables;
   // scratch
   DevBuf ch_rows, ch_vals, alt_rows, alt_vals, uq_rows, uq_vals, new_vals;
-  DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt;
+  DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt, sorted_rows;
+
+  // Sort m rows in place by layer key (word 0, then a mix of the other words).
+  void sort_by_layer_key(int W, u64* rows, u32 m) {
+    if (m < 2) return;
+    keys.reserve(sizeof(u64) * 2 * m);
+    ch_vals.reserve(sizeof(u32) * m);
+    sorted_rows.reserve(sizeof(u64) * W * m);
+    launch_layer_keys(W, rows, m, keys.as<u64>(), stream);
+    launch_iota(ch_vals.as<u32>(), m, stream);
+    sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), m);
+    launch_gather_rows(W, rows, ch_vals.as<u32>(), m, sorted_rows.as<u64>(), stream);
+    SW_CUDA(cudaMemcpyAsync(rows, sorted_rows.p, sizeof(u64) * W * m, cudaMemcpyDeviceToDevice, stream));
+    count_launch(4);
+  }
   Side F, B;
   sw_stats* st = nullptr;
 
@@ -267,10 +281,15 @@ class Engine {
     launch_iota(ch_vals.as<u32>(), Nc, stream);
     count_launch(2);
     if (st) st->subsets_expanded += N;
-    sort_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc);
-    launch_unique_flags(W, ch_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
-    count_launch();
-    const u32 u = compact(W, ch_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
+    // sort the children by layer key (2 words), then gather the rows in that order
+    keys.reserve(sizeof(u64) * 2 * N);
+    sorted_rows.reserve(sizeof(u64) * W * N);
+    launch_layer_keys(W, ch_rows.as<u64>(), Nc, keys.as<u64>(), stream);
+    sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
+    launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
+    launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
+    count_launch(3);
+    const u32 u = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
                           uq_vals.as<u32>());
     // dominance: visited set inside the child, or a proper subset in the layer
     launch_fill_u32(flags_a.as<u32>(), 0, u, stream);
@@ -320,7 +339,7 @@ class Engine {
     // visited := visited ∪ layer (both sorted, disjoint)
     X.vis_alt.reserve(sizeof(u64) * W * ((size_t)X.vis_count + f + 1));
     timed(3, (double)(X.vis_count + f) * 8.0 * W * 2, [&] {
-      launch_merge(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
+      launch_merge_key(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
     });
     count_launch();
     std::swap(X.vis.p, X.vis_alt.p);
@@ -437,9 +456,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       // for complements; sort them properly via the row sort.
       SW_CUDA(cudaMemcpyAsync(E.B.vis.p, E.B.rows.p, sizeof(u64) * W * seeds.size(), cudaMemcpyDeviceToDevice,
                               E.stream));
-      E.keep.reserve(sizeof(u32) * seeds.size());
-      launch_iota(E.keep.as<u32>(), (u32)seeds.size(), E.stream);
-      E.sort_rows(W, E.B.vis.as<u64>(), E.keep.as<u32>(), (u32)seeds.size());
+      E.sort_by_layer_key(W, E.B.vis.as<u64>(), (u32)seeds.size());
       E.B.vis_count = (u32)seeds.size();
       E.build_tree(W, E.B.vis.as<u64>(), E.B.vis_count, E.B.vis_gamma, E.B.vis_split);
     }

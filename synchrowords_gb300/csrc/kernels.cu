@@ -240,9 +240,40 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(const u32* __restri
 
 size_t scan_temp_bytes(u32 n) { return sizeof(u32) * ((n + kScanTile - 1) / kScanTile + 1); }
 
+// Small arrays: one block walks the array tile by tile with a carry.
+__global__ void __launch_bounds__(kScanThreads) k_scan_onepass(const u32* __restrict__ in, u32* __restrict__ out,
+                                                               u32 n, u32* total_dev) {
+  u32 carry = 0;
+  for (u32 base = 0; base < n; base += kScanTile) {
+    u32 v[kScanItems];
+    u32 s = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      u32 idx = base + threadIdx.x * kScanItems + j;
+      v[j] = idx < n ? in[idx] : 0;
+      s += v[j];
+    }
+    u32 tot;
+    u32 run = carry + block_exclusive_scan(s, tot);
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+      u32 idx = base + threadIdx.x * kScanItems + j;
+      if (idx < n) out[idx] = run;
+      run += v[j];
+    }
+    carry += tot;
+  }
+  if (threadIdx.x == 0 && total_dev) *total_dev = carry;
+}
+
 void launch_scan(const u32* in, u32* out, u32 n, u32* total_dev, void* temp, cudaStream_t s) {
   if (n == 0) {
     if (total_dev) SW_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(u32), s));
+    return;
+  }
+  if (n <= 8 * kScanTile) {
+    k_scan_onepass<<<1, kScanThreads, 0, s>>>(in, out, n, total_dev);
+    SW_LAUNCH_CHECK();
     return;
   }
   u32 nb = (n + kScanTile - 1) / kScanTile;
@@ -900,6 +931,74 @@ __global__ void k_merge(const u64* __restrict__ A, u32 na, const u64* __restrict
 void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s) {
   if (na + nb == 0) return;
   SW_DISPATCH_W(W, (k_merge<WW><<<(na + nb + 255) / 256, 256, 0, s>>>(A, na, B, nb, out)));
+  SW_LAUNCH_CHECK();
+}
+
+// ===========================================================================
+// Layer keys: (word 0, 32-bit mix of words 1..W-1).  Sorting by this key
+// groups sets by their most frequent states (word 0) and makes equal sets
+// adjacent; distinct sets with equal keys are possible only through a hash
+// collision, which can at worst leave a duplicate in a layer (harmless).
+// ===========================================================================
+template <int W>
+__device__ __forceinline__ u64 rest_mix(const u64* r) {
+  u64 h = 0x9E3779B97F4A7C15ULL;
+#pragma unroll
+  for (int w = 1; w < W; ++w) {
+    u64 x = r[w] ^ (h + 0x632BE59BD9B4E019ULL * (u64)w);
+    x ^= x >> 31;
+    x *= 0x94D049BB133111EBULL;
+    x ^= x >> 29;
+    h = (h ^ x) * 0xBF58476D1CE4E5B9ULL;
+  }
+  return W > 1 ? (h ^ (h >> 32)) << 32 : 0ULL;
+}
+
+template <int W>
+__global__ void k_layer_keys(const u64* __restrict__ rows, u32 m, u64* __restrict__ keys) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  u64 r[W];
+#pragma unroll
+  for (int w = 0; w < W; ++w) r[w] = rows[(size_t)i * W + w];
+  keys[2 * (size_t)i] = r[0];
+  keys[2 * (size_t)i + 1] = rest_mix<W>(r);
+}
+
+void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_layer_keys<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, keys)));
+  SW_LAUNCH_CHECK();
+}
+
+// Merge of two arrays sorted by layer key (A first on equal keys).
+template <int W>
+__global__ void k_merge_key(const u64* __restrict__ A, u32 na, const u64* __restrict__ B, u32 nb,
+                            u64* __restrict__ out) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= na + nb) return;
+  const bool fromA = i < na;
+  const u64* x = fromA ? A + (size_t)i * W : B + (size_t)(i - na) * W;
+  const u64 x0 = x[0], x1 = rest_mix<W>(x);
+  const u64* other = fromA ? B : A;
+  u32 lo = 0, hi = fromA ? nb : na;
+  while (lo < hi) {
+    const u32 mid = (lo + hi) >> 1;
+    const u64* y = other + (size_t)mid * W;
+    const u64 y0 = y[0], y1 = rest_mix<W>(y);
+    // A element: count B keys strictly less; B element: count A keys <= its key
+    const bool before = fromA ? (y0 < x0 || (y0 == x0 && y1 < x1)) : (y0 < x0 || (y0 == x0 && y1 <= x1));
+    if (before) lo = mid + 1;
+    else hi = mid;
+  }
+  const size_t pos = (size_t)(fromA ? i : i - na) + lo;
+#pragma unroll
+  for (int w = 0; w < W; ++w) out[pos * W + w] = x[w];
+}
+
+void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s) {
+  if (na + nb == 0) return;
+  SW_DISPATCH_W(W, (k_merge_key<WW><<<(na + nb + 255) / 256, 256, 0, s>>>(A, na, B, nb, out)));
   SW_LAUNCH_CHECK();
 }
 

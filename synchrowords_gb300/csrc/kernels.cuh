@@ -92,6 +92,12 @@ void launch_popcount(int W, const u64* rows, u32 m, u32* out, cudaStream_t s);
 // flags[i] = AND/OR combine: out[i] = (a[i] == 0 && b[i] == 0).
 void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t s);
 
+// Layer keys keys[2i..2i+1] = (word 0 of row i, 32-bit mix of its other
+// words in the high half): sort order of a layer and of the visited list.
+void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s);
+// Merge of two row arrays sorted by layer key.
+void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);
+
 // p[i] = i.
 void launch_iota(u32* p, u32 m, cudaStream_t s);
 
