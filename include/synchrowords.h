@@ -213,6 +213,34 @@ int sw_subsets_check(sw_context* ctx, uint32_t n, const uint64_t* sets, uint64_t
  * sort_keep_unique (synchrolib/utils/vector.hpp:13-27). */
 int sw_sort_unique(sw_context* ctx, uint32_t n, uint64_t* sets, uint64_t count, uint64_t* out_count);
 
+/* ---- allocation-free variant --------------------------------------------
+ * No counterpart in the reference (its GPU helpers cudaMalloc and cudaFree
+ * on every call, preprocessed_transition_kernel.cu:65-87).
+ *
+ * For callers that must not have the library allocate device memory — an
+ * application whose own pool allocator owns the device budget, or a service
+ * that forbids allocation while it serves requests.  Same check as
+ * sw_subsets_check, but on device buffers the caller owns and with no
+ * cudaMalloc / cudaFree / allocating library call: the scratch it needs (the
+ * AND masks of the set list's row tiles) is a static device array of the
+ * library, sized for SW_NOALLOC_MAX_SETS sets (about 1 MB; every GPU that
+ * loads the library keeps it until the process exits).  Larger set lists are
+ * rejected with SW_ERR_CAPACITY.
+ *
+ * Rows use the device layout: W = 1, 2, 4 or 8 uint64 words for n <= 64, 128,
+ * 256, 512; state q is bit (63 - q % 64) of word q / 64; unused bits are 0.
+ * d_results[i] (uint32) becomes 1 if some d_sets row ⊆ d_checks row i
+ * (⊊ when proper), else 0.  The work is queued on `stream` (NULL = default
+ * stream); the call returns without waiting for it.  The first call on a
+ * device looks up the scratch array's device address with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the one scratch array and each overwrites it: calls that can run at the
+ * same time on the GPU race and must be ordered by the caller.  Errors are
+ * reported like every other entry point (status code + sw_last_error()). */
+#define SW_NOALLOC_MAX_SETS (1u << 20)
+int sw_subsets_check_device_noalloc(uint32_t n, const uint64_t* d_sets, uint64_t set_count, const uint64_t* d_checks,
+                                    uint64_t check_count, int32_t proper, uint32_t* d_results, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,9 @@ def load_library():
     lib.sw_sort_unique.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P]
     lib.sw_solve_batch.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
                                    ctypes.POINTER(_Result), ctypes.c_uint32]
+    lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
+                                                     ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
+                                                     ctypes.c_void_p, ctypes.c_void_p]
     lib.sw_profile_begin.argtypes = [ctypes.c_void_p]
     lib.sw_profile_end.argtypes = [ctypes.c_void_p, ctypes.POINTER(_KernelProfile)]
     lib.sw_context_stream.argtypes = [ctypes.c_void_p]

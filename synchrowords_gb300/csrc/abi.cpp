@@ -55,6 +55,10 @@ void set_name(char* dst, const char* src) {
 
 }  // namespace
 
+namespace sw {
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+}  // namespace sw
+
 extern "C" {
 
 const char* sw_version(void) { return "synchrowords-gb300 0.1.0 (sm_103a)"; }

@@ -1,0 +1,73 @@
+"""The allocation-free subset check (sw_subsets_check_device_noalloc).
+
+Callers that own the whole device budget through their own allocator, or that
+may not allocate while serving, pass their own device buffers; the library
+uses only its static scratch array.  This file checks that entry point
+against the allocating one (sw_subsets_check) on the same inputs, for two
+calls in a row (the second reuses the scratch the first left behind), and
+that an oversized set list is refused before any device work.  It is named to
+run last so that a failure here leaves every other test already run.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from bitsets import random_sets, to_rows
+
+pytestmark = pytest.mark.gpu
+
+
+def device_rows(sets, n):
+    """Rows in the device layout: W in {1, 2, 4, 8} words, state q at bit 63 - q % 64 of word q / 64."""
+    w = (n + 63) // 64
+    W = 1 if w <= 1 else 2 if w <= 2 else 4 if w <= 4 else 8
+    out = np.zeros((len(sets), W), dtype=np.uint64)
+    for i, s in enumerate(sets):
+        for q in s:
+            out[i, q // 64] |= np.uint64(1 << (63 - q % 64))
+    return out
+
+
+def run_noalloc(lib, n, sets, checks, proper):
+    import torch
+    ds = torch.from_numpy(device_rows(sets, n).view(np.int64)).cuda()
+    dc = torch.from_numpy(device_rows(checks, n).view(np.int64)).cuda()
+    res = torch.full((len(checks),), 7, dtype=torch.int32, device="cuda")  # not zero: the call must clear it
+    stream = torch.cuda.current_stream()
+    rc = lib.sw_subsets_check_device_noalloc(n, ds.data_ptr(), len(sets), dc.data_ptr(), len(checks),
+                                             int(proper), res.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+    assert rc == 0, lib.sw_last_error().decode()
+    torch.cuda.synchronize()
+    return res.cpu().numpy().astype(np.uint8).tolist()
+
+
+def test_noalloc_matches_allocating_entry_point_twice(ctx, native_lib):
+    rng = np.random.default_rng(2024)
+    cases = []
+    # first call: 200 states, plain subsets; second: 96 states, proper subsets,
+    # fewer sets, so stale masks from the first call would show if reused
+    n1 = 200
+    S1 = random_sets(rng, n1, 3000, 0.1) + random_sets(rng, n1, 300, 0.4)
+    C1 = random_sets(rng, n1, 2000, 0.75) + S1[:50]
+    cases.append((n1, S1, C1, False))
+    n2 = 96
+    S2 = random_sets(rng, n2, 700, 0.15)
+    C2 = random_sets(rng, n2, 900, 0.6) + S2[:30] + [frozenset(range(n2))]
+    cases.append((n2, S2, C2, True))
+    for n, S, C, proper in cases:
+        want = ctx.subsets_check(n, to_rows(S, n), to_rows(C, n), proper=proper).tolist()
+        got = run_noalloc(native_lib, n, S, C, proper)
+        assert got == want
+        assert 0 < sum(got) < len(got)  # both outcomes occur
+
+
+def test_noalloc_rejects_oversized_set_list(native_lib):
+    import torch
+    dummy = torch.zeros(8, dtype=torch.int64, device="cuda")
+    res = torch.zeros(1, dtype=torch.int32, device="cuda")
+    too_many = (1 << 20) + 1
+    rc = native_lib.sw_subsets_check_device_noalloc(64, dummy.data_ptr(), too_many, dummy.data_ptr(), 1, 0,
+                                                    res.data_ptr(), None)
+    assert rc == -7  # SW_ERR_CAPACITY, refused before touching the buffers
+    assert b"SW_NOALLOC_MAX_SETS" in native_lib.sw_last_error()
