@@ -35,16 +35,33 @@ sys.path.insert(0, str(ROOT))
 
 PLAN_EXACT = json.dumps({"algorithms": [{"name": "Exact", "config": {}}]})
 
+# configs/exact.json of the reference without its Brute / Eppstein entries
+PLAN_BEAM_EXACT = json.dumps({
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1",
+    "algorithms": [
+        {"name": "Beam", "config": {"presort": "indeg", "dynamic": True,
+                                    "min_beam_size": "AUT_N * std::log2(AUT_N)",
+                                    "max_beam_size": "AUT_N * AUT_N * std::log2(AUT_N)",
+                                    "beam_exact_ratio": 0.01}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
+
 WORKLOADS = {
-    # name: (n, k, count, description)
-    "n200": (200, 2, 16, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
-    "n48": (48, 2, 64, "plain exact, 64 random binary DFAs, n=48 (64-bit sets)"),
+    # name: (n, k, count, plan, description); n = 0 marks the uneven batch
+    "n200": (200, 2, 16, PLAN_EXACT, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
+    "n48": (48, 2, 64, PLAN_EXACT, "plain exact, 64 random binary DFAs, n=48 (64-bit sets)"),
+    "batch4096": (0, 0, 4096, PLAN_EXACT,
+                  "plain exact, 4096 random DFAs, n ~ U[32,160], k ~ U{2,3} (64/128/256-bit sets)"),
+    "n320": (320, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=320"),
+    "n384": (384, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=384"),
 }
 
 
 def workload_dfas(name: str, rank: int):
-    from synchrowords_gb300.generate import random_dfa
-    n, k, count, _ = WORKLOADS[name]
+    from synchrowords_gb300.generate import batch, random_dfa
+    n, k, count, _, _ = WORKLOADS[name]
+    if n == 0:
+        return batch(count, 2026 + rank)
     base = 1 + rank * 100000
     return [(n, k, random_dfa(n, k, base + i)) for i in range(count)]
 
@@ -136,14 +153,23 @@ def barrier(world: int):
         dist.barrier()
 
 
-def cpu_baseline(dfas, sample: int, threads: int):
-    """Oracle (CPU restatement of the reference's Exact) on the first `sample` DFAs."""
+def cpu_baseline(dfas, sample: int, threads: int, plan: str = PLAN_EXACT):
+    """Oracle (CPU restatement of the reference) running `plan` on the first `sample` DFAs."""
+    import math
     import oracle
     oracle.build()
     t0 = time.perf_counter()
     lengths = []
     for n, k, d in dfas[:sample]:
-        r = oracle.exact(d, n, k, oracle.ExactParams(threads=threads))
+        if plan == PLAN_BEAM_EXACT:
+            lg = math.log2(n)
+            b = oracle.beam(d, n, k, oracle.BeamParams(dynamic=True, presort_indeg=True, min_beam_size=int(n * lg),
+                                                       max_beam_size=int(n * n * lg)), upper=(n - 1) ** 2 + 1)
+            r = oracle.exact(d, n, k, oracle.ExactParams(dfs_min_list_size=8192, bfs_small_list_size=n * k,
+                                                         max_memory_mb=12 * 1024, threads=threads),
+                             upper=b.upper)
+        else:
+            r = oracle.exact(d, n, k, oracle.ExactParams(threads=threads))
         lengths.append(r.upper)
     dt = time.perf_counter() - t0
     return dt * 1000.0 / sample, lengths
@@ -155,21 +181,22 @@ def run_reference(args, world, rank):
     dfas = workload_dfas(args.workload, 0)
     threads = max(1, min(64, os.cpu_count() or 1))
     per_step = max(1, min(len(dfas), args.ref_sample))
+    n, k, count, plan, desc = WORKLOADS[args.workload]
     for w in range(args.warmup):
-        cpu_baseline(dfas[w % len(dfas):] + dfas, 1, threads)
+        cpu_baseline(dfas[w % len(dfas):] + dfas, 1, threads, plan)
     times = []
     for s in range(args.steps):
         sub = [dfas[(s * per_step + i) % len(dfas)] for i in range(per_step)]
-        ms, _ = cpu_baseline(sub, per_step, threads)
+        ms, _ = cpu_baseline(sub, per_step, threads, plan)
         times.append(ms)
     value = sum(times) / len(times)
-    n, k, count, desc = WORKLOADS[args.workload]
     line = {
         "impl": "reference", "metric": "time-to-exact reset length per random DFA", "value": round(value, 4),
         "unit": "ms", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(value * per_step, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step": per_step, "plan": "Exact (defaults)",
+        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step": per_step,
+                   "plan": "Exact (defaults)" if plan == PLAN_EXACT else "Beam(dynamic)+Exact",
                    "l2": "host-only run"},
         "cpu_baseline": {"value": round(value, 4), "unit": "ms", "cores": threads, "kind": "port",
                          "sample": f"{per_step} DFAs per step out of {count}, rotating"},
@@ -185,7 +212,7 @@ def run_ours(args, world, rank, local):
     nb.build()
     torch.cuda.set_device(local)
     dfas = workload_dfas(args.workload, rank)
-    n, k, count, desc = WORKLOADS[args.workload]
+    n, k, count, plan, desc = WORKLOADS[args.workload]
     ctx = sw.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -193,7 +220,7 @@ def run_ours(args, world, rank, local):
     def one_step():
         launches = 0
         lengths = []
-        for r in ctx.solve_batch(dfas, PLAN_EXACT, workers=args.streams):
+        for r in ctx.solve_batch(dfas, plan, workers=args.streams):
             launches += r.stats["kernel_launches"]
             lengths.append(r.upper)
             if r.word is None or len(r.word) != r.upper:
@@ -235,7 +262,7 @@ def run_ours(args, world, rank, local):
     ctx.profile_begin()
     pairs = 0
     for (nn, kk, d) in dfas:
-        r = ctx.solve(d, nn, kk, PLAN_EXACT)
+        r = ctx.solve(d, nn, kk, plan)
         pairs += r.stats["logical_pairs"]
     prof = ctx.profile_end()
     peak, peak_kind = load_peaks()
@@ -257,7 +284,7 @@ def run_ours(args, world, rank, local):
     if world == 1 and not args.no_cpu_baseline:
         threads = max(1, min(64, os.cpu_count() or 1))
         sample = min(args.cpu_sample, count)
-        cpu_ms, cpu_len = cpu_baseline(dfas, sample, threads)
+        cpu_ms, cpu_len = cpu_baseline(dfas, sample, threads, plan)
         if cpu_len != lengths[:sample]:
             raise RuntimeError(f"length mismatch vs oracle: {cpu_len} != {lengths[:sample]}")
         cpu = {"value": round(cpu_ms, 3), "unit": "ms", "cores": threads, "kind": "port",
@@ -269,7 +296,7 @@ def run_ours(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dev_total / args.steps, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": "Exact (defaults)",
+        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": "Exact (defaults)" if plan == PLAN_EXACT else "Beam(dynamic)+Exact",
                    "streams": args.streams,
                    "l2": "flushed (256 MB write) before every timed step", "per_gpu_ms_per_dfa": round(value, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

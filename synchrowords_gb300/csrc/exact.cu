@@ -261,7 +261,9 @@ class Engine {
   }
 
   // One BFS layer on side X (forward = image, backward = preimage of complements).
-  void step(Side& X, bool forward, int W, int n, int k) {
+  // With `dominance` false only duplicates are removed and the visited list is
+  // left alone (the bounded inverse phase, see Solver::exact).
+  void step(Side& X, bool forward, int W, int n, int k, bool dominance = true) {
     const u32 m = X.count;
     const u64 N = (u64)m * k;
     if (N > 0xffffffffULL) throw std::runtime_error("layer exceeds 2^32 children");
@@ -291,6 +293,26 @@ class Engine {
     count_launch(3);
     const u32 u = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
                           uq_vals.as<u32>());
+    if (!dominance) {
+      // bounded phase: the deduplicated layer is the new frontier as is
+      std::swap(X.rows.p, uq_rows.p);
+      std::swap(X.rows.cap, uq_rows.cap);
+      X.count = u;
+      if (st) {
+        st->subsets_kept += u;
+        st->dfs_sets += u;
+      }
+      auto L = std::make_unique<Layer>();
+      L->origin.reserve(sizeof(u32) * std::max<u32>(u, 1));
+      if (u) SW_CUDA(cudaMemcpyAsync(L->origin.p, uq_vals.p, sizeof(u32) * u, cudaMemcpyDeviceToDevice, stream));
+      L->count = u;
+      L->parent_count = m;
+      X.layers.push_back(std::move(L));
+      if (verbose)
+        std::fprintf(stderr, "[sw] %s (bounded) parents=%u children=%u unique=%u | %.3f ms\n",
+                     forward ? "BFS " : "IBFS", m, Nc, u, vclock() - t_step0);
+      return;
+    }
     // dominance: visited set inside the child, or a proper subset in the layer
     launch_fill_u32(flags_a.as<u32>(), 0, u, stream);
     launch_fill_u32(flags_b.as<u32>(), 0, u, stream);
@@ -470,8 +492,20 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
   u64 rt = 0;
   bool found = false, oom = false;
   u32 wit_q = 0, wit_s = 0;
+  // Bounded inverse phase (the device counterpart of the reference's DFS
+  // shortcut, dfs.cpp:64-218 and meet_in_the_middle.cpp:466-511): when the
+  // upper bound is backed by a word, only lengths < bound remain to be
+  // excluded.  F is then frozen and B is expanded level by level with
+  // duplicate removal only, each level meet-checked against F.  The switch is
+  // taken when the projected cost of those levels (measured per-query meet
+  // time, B growing by the last observed branching) is below that of
+  // continuing the dominance-pruned search (last step's time growing 1.6x per
+  // step), and the widest projected level fits the memory budget.
+  bool bounded = false;
+  double t_iter_last = 0, t_meet_per_query = 0, b_growth = k * 0.95;
   while (rt < max_rt) {  // meet_in_the_middle.cpp:73
-    const bool fwd = E.F.count <= E.B.count;
+    const auto t_iter0 = std::chrono::steady_clock::now();
+    const bool fwd = bounded ? false : E.F.count <= E.B.count;
     Side& X = fwd ? E.F : E.B;
     size_t live = (size_t)(E.F.count + E.F.vis_count + E.B.count + E.B.vis_count) * row_bytes;
     size_t next = (size_t)X.count * k * (3 * row_bytes + 4 * sizeof(u32));
@@ -480,7 +514,9 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       break;
     }
     rt++;
-    E.step(X, fwd, W, n, k);
+    const u32 parents_before = X.count;
+    E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
+    if (!fwd && parents_before) b_growth = std::max(1.0, (double)E.B.count / parents_before);
     if (fwd) {
       st.bfs_steps++;
       E.build_tree(W, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split);
@@ -489,13 +525,40 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     }
     // meet check: some F disjoint from some B-complement (F ⊆ B)
     const double t_meet0 = E.vclock();
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    const auto t_meet_host0 = std::chrono::steady_clock::now();
     SW_CUDA(cudaMemsetAsync(E.d_misc, 0, 4 * sizeof(u32), E.stream));
     E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split, E.B.rows.as<u64>(), E.B.count,
             n, nullptr, true);
     st.meet_pairs += (u64)E.F.count * E.B.count;
     SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
     SW_CUDA(cudaStreamSynchronize(E.stream));
+    const auto t_end = std::chrono::steady_clock::now();
     const u32* w = E.pinned.as<u32>();
+    t_iter_last = std::chrono::duration<double>(t_end - t_iter0).count();
+    if (E.B.count)
+      t_meet_per_query = std::chrono::duration<double>(t_end - t_meet_host0).count() / (double)E.B.count;
+    if (!bounded && b.has_word && !w[0] && rt < max_rt && rt >= 4 && E.B.count) {
+      const u64 R = max_rt - rt;  // levels still to exclude
+      const double per_row = t_meet_per_query + 5e-9;  // meet check + dedup per child
+      double lvl = E.B.count, total = 0, mitm = 0, grow = 1.0;
+      bool fits = true;
+      for (u64 i = 1; i <= R && fits; ++i) {
+        lvl *= b_growth;
+        total += lvl * k * per_row;
+        grow *= 1.6;
+        mitm += t_iter_last * grow;
+        if ((lvl * k * (3.0 * row_bytes + 16) + (double)(E.F.count + E.B.count) * row_bytes) > (double)budget)
+          fits = false;
+      }
+      if (fits && total < mitm) {
+        bounded = true;
+        if (E.verbose)
+          std::fprintf(stderr, "[sw] bounded phase from length %llu: %llu levels left, |F|=%u |B|=%u, "
+                       "projected %.1f ms vs %.1f ms\n", (unsigned long long)rt, (unsigned long long)R, E.F.count,
+                       E.B.count, 1e3 * total, 1e3 * mitm);
+      }
+    }
     if (E.verbose)
       std::fprintf(stderr, "[sw] len %llu: |F|=%u |B|=%u meet check %.3f ms%s\n", (unsigned long long)rt, E.F.count,
                    E.B.count, E.vclock() - t_meet0, w[0] ? " -> found" : "");
