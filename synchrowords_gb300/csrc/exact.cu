@@ -47,8 +47,10 @@ struct Side {
   DevBuf gamma, split;  // tree over `rows` (kept for F only)
   std::vector<std::unique_ptr<Layer>> layers;
   std::vector<u64> seed_states;  // backward side: the state of each seed row
+  double unique_growth = 0;      // distinct children per parent at the last step
   void reset() {
     count = vis_count = 0;
+    unique_growth = 0;
     layers.clear();
     seed_states.clear();
   }
@@ -293,6 +295,7 @@ class Engine {
     count_launch(3);
     const u32 u = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
                           uq_vals.as<u32>());
+    if (m) X.unique_growth = (double)u / m;  // branching before dominance pruning
     if (!dominance) {
       // bounded phase: the deduplicated layer is the new frontier as is
       std::swap(X.rows.p, uq_rows.p);
@@ -516,7 +519,9 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     rt++;
     const u32 parents_before = X.count;
     E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
-    if (!fwd && parents_before) b_growth = std::max(1.0, (double)E.B.count / parents_before);
+    // projected branching of the bounded levels: distinct children per parent
+    // before pruning, never below 1.5, plus 10% margin
+    if (!fwd && parents_before) b_growth = 1.1 * std::max(1.5, E.B.unique_growth);
     if (fwd) {
       st.bfs_steps++;
       E.build_tree(W, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split);
@@ -540,16 +545,19 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       t_meet_per_query = std::chrono::duration<double>(t_end - t_meet_host0).count() / (double)E.B.count;
     if (!bounded && b.has_word && !w[0] && rt < max_rt && rt >= 4 && E.B.count) {
       const u64 R = max_rt - rt;  // levels still to exclude
-      const double per_row = t_meet_per_query + 5e-9;  // meet check + dedup per child
+      // per child: dedup (~1 ns measured at 10^7 rows) + the meet check's cost per query
+      const double per_row = t_meet_per_query + 2e-9;
       double lvl = E.B.count, total = 0, mitm = 0, grow = 1.0;
       bool fits = true;
       for (u64 i = 1; i <= R && fits; ++i) {
-        lvl *= b_growth;
-        total += lvl * k * per_row;
+        const double children = lvl * k;
+        total += children * per_row;
         grow *= 1.6;
         mitm += t_iter_last * grow;
-        if ((lvl * k * (3.0 * row_bytes + 16) + (double)(E.F.count + E.B.count) * row_bytes) > (double)budget)
+        // children rows + their sorted copy + the kept level, keys and payloads
+        if (children * (3.0 * row_bytes + 32) + (lvl + (double)E.F.count) * row_bytes > (double)budget)
           fits = false;
+        lvl *= b_growth;
       }
       if (fits && total < mitm) {
         bounded = true;
