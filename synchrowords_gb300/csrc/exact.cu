@@ -373,6 +373,51 @@ class Engine {
     build_tree(W, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split);
   }
 
+  // Bounded phase helpers.  expand_dedup: preimages (complement rows) of m
+  // parents, duplicates removed, into out_rows / out_origin (origin = letter *
+  // m + parent) — no dominance, no visited update.
+  void expand_dedup(const u64* parents, u32 m, int W, int k, DevBuf& out_rows, DevBuf& out_origin, u32& out_count) {
+    const u64 N = (u64)m * k;
+    if (N > 0xffffffffULL) throw std::runtime_error("level exceeds 2^32 children");
+    const u32 Nc = (u32)N;
+    ch_rows.reserve(sizeof(u64) * W * N);
+    ch_vals.reserve(sizeof(u32) * N);
+    flags_a.reserve(sizeof(u32) * N);
+    keys.reserve(sizeof(u64) * 2 * N);
+    sorted_rows.reserve(sizeof(u64) * W * N);
+    out_rows.reserve(sizeof(u64) * W * std::max<u64>(N, 1));
+    out_origin.reserve(sizeof(u32) * std::max<u64>(N, 1));
+    const double t0 = vclock();
+    timed(1, (double)m * 8.0 * W * (1 + k), [&] { launch_expand(W, false, parents, m, tables, ch_rows.as<u64>(), stream); });
+    launch_iota(ch_vals.as<u32>(), Nc, stream);
+    launch_layer_keys(W, ch_rows.as<u64>(), Nc, keys.as<u64>(), stream);
+    sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
+    launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
+    launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
+    count_launch(5);
+    if (st) st->subsets_expanded += N;
+    out_count = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, out_rows.as<u64>(),
+                        out_origin.as<u32>());
+    if (verbose)
+      std::fprintf(stderr, "[sw] IBFS (bounded) parents=%u children=%u unique=%u | %.3f ms\n", m, Nc, out_count,
+                   vclock() - t0);
+  }
+
+  // Meet check of q complement rows against F; on a hit returns true with the
+  // query index and the F index.
+  bool meet(int W, int n, const u64* Q, u32 q, u32* qi, u32* si) {
+    SW_CUDA(cudaMemsetAsync(d_misc, 0, 4 * sizeof(u32), stream));
+    query(W, kQueryDisjoint, F.rows.as<u64>(), F.count, F.gamma, F.split, Q, q, n, nullptr, true);
+    if (st) st->meet_pairs += (u64)F.count * q;
+    SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaStreamSynchronize(stream));
+    const u32* w = pinned.as<u32>();
+    if (!w[0]) return false;
+    *qi = w[1];
+    *si = w[2];
+    return true;
+  }
+
   // Trace letters of set `idx` at the top layer of side X down to depth 0.
   std::vector<uint32_t> trace(const Side& X, u32 idx, u32* seed_index) {
     std::vector<uint32_t> letters;  // from the top layer down
@@ -386,6 +431,96 @@ class Engine {
     return letters;
   }
 };
+
+// ---------------------------------------------------------------------------
+// Bounded inverse phase with chunking (the reference's memory-bounded DFS,
+// dfs.cpp:161-218, on device levels).  F is frozen; B levels are expanded
+// with duplicate removal only and meet-checked against F.  A level whose
+// children fit the budget is expanded whole (plain BFS); otherwise its
+// parents are taken in chunks and each chunk's subtree is explored depth
+// first.  A hit at length L makes every other branch search only lengths
+// below L (dfs.cpp:179-189), so the smallest length found is the answer.
+// ---------------------------------------------------------------------------
+namespace {
+struct DLevel {
+  DevBuf rows, origin;
+  u32 count = 0;
+  u32 chunk_off = 0, chunk_cnt = 0;  // parent slice this level was expanded from
+};
+
+struct BoundedSearch {
+  Engine& E;
+  const Automaton& A;
+  int W, n, k;
+  size_t budget, row_bytes;
+  u64 min_chunk;
+  u64 max_len;  // longest length still worth examining
+  u64 best = 0;
+  std::vector<uint32_t> best_tail;  // letters after the forward part, for the best hit
+  u32 best_f = 0;
+  std::vector<DLevel*> levels;                // levels[0] stands for E.B (nullptr)
+  std::vector<std::unique_ptr<DLevel>> pool;  // one reusable level per depth
+  sw_stats& st;
+
+  size_t held() const {
+    size_t s = (size_t)(E.F.count + E.F.vis_count + E.B.count + E.B.vis_count) * row_bytes;
+    for (size_t i = 1; i < levels.size(); ++i) s += (size_t)levels[i]->count * (row_bytes + 4);
+    return s;
+  }
+
+  const u64* level_rows(size_t li) const {
+    return li == 0 ? E.B.rows.as<u64>() : levels[li]->rows.as<u64>();
+  }
+
+  // Letters from level `li` index x back to the B frontier, plus the MITM B trace.
+  std::vector<uint32_t> tail_word(size_t li, u32 x) {
+    std::vector<uint32_t> letters;
+    for (size_t l = li; l >= 1; --l) {
+      const DLevel& L = *levels[l];
+      const u32 o = E.read_u32(L.origin.as<u32>() + x);
+      letters.push_back(o / L.chunk_cnt);
+      x = L.chunk_off + o % L.chunk_cnt;
+    }
+    std::vector<uint32_t> bw = E.trace(E.B, x, nullptr);
+    letters.insert(letters.end(), bw.begin(), bw.end());
+    return letters;
+  }
+
+  // Explore the children of parents [off, off+cnt) of level li (at length len).
+  void explore(size_t li, u32 off, u32 cnt, u64 len) {
+    if (len + 1 > max_len || cnt == 0) return;
+    const double per_child = (double)k * (3.0 * row_bytes + 32) + (double)k * (row_bytes + 4);
+    const size_t have = budget > held() ? budget - held() : 0;
+    u64 chunk = (u64)((double)have / per_child);
+    if (chunk < min_chunk) chunk = min_chunk;
+    if (chunk > cnt) chunk = cnt;
+    for (u32 pos = 0; pos < cnt && len + 1 <= max_len; pos += (u32)chunk) {
+      const u32 c = (u32)std::min<u64>(chunk, cnt - pos);
+      const size_t me = levels.size();
+      while (pool.size() <= me) pool.push_back(std::make_unique<DLevel>());
+      DLevel* L = pool[me].get();
+      L->chunk_off = off + pos;
+      L->chunk_cnt = c;
+      E.expand_dedup(level_rows(li) + (size_t)(off + pos) * W, c, W, k, L->rows, L->origin, L->count);
+      st.dfs_sets += L->count;
+      levels.push_back(L);
+      u32 q = 0, s = 0;
+      if (E.meet(W, n, levels[me]->rows.as<u64>(), levels[me]->count, &q, &s)) {
+        best = len + 1;
+        best_f = s;
+        best_tail = tail_word(me, q);
+        max_len = len;  // only shorter words are of interest from now on
+        if (E.verbose)
+          std::fprintf(stderr, "[sw] bounded search: word of length %llu found; searching below\n",
+                       (unsigned long long)best);
+      } else if (len + 1 < max_len) {
+        explore(me, 0, levels[me]->count, len + 1);
+      }
+      levels.pop_back();
+    }
+  }
+};
+}  // namespace
 
 Solver::Solver(int device) : device_(device), eng_(new Engine(device)) {}
 Solver::~Solver() = default;
@@ -513,6 +648,16 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     size_t live = (size_t)(E.F.count + E.F.vis_count + E.B.count + E.B.vis_count) * row_bytes;
     size_t next = (size_t)X.count * k * (3 * row_bytes + 4 * sizeof(u32));
     if (live + next > budget) {
+      // meet_in_the_middle.cpp:98-101 + exact.cpp:139-145: out of memory, the
+      // search continues in the memory-bounded inverse phase when DFS is
+      // enabled and the remaining depth is bounded (word-backed bound or at
+      // most 64 levels); otherwise only a lower bound results
+      if (cfg.dfs && !bounded && E.B.count && (b.has_word || max_rt - rt <= 64)) {
+        bounded = true;
+        if (E.verbose)
+          std::fprintf(stderr, "[sw] memory budget reached at length %llu: bounded phase\n", (unsigned long long)rt);
+        break;
+      }
       oom = true;
       break;
     }
@@ -521,7 +666,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
     // projected branching of the bounded levels: distinct children per parent
     // before pruning, never below 1.5, plus 10% margin
-    if (!fwd && parents_before) b_growth = 1.1 * std::max(1.5, E.B.unique_growth);
+    if (!fwd && parents_before) b_growth = std::max(1.2, E.B.unique_growth);
     if (fwd) {
       st.bfs_steps++;
       E.build_tree(W, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split);
@@ -559,7 +704,8 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
           fits = false;
         lvl *= b_growth;
       }
-      if (fits && total < mitm) {
+      (void)fits;  // over-budget levels are taken in chunks (BoundedSearch)
+      if (total < mitm) {
         bounded = true;
         if (E.verbose)
           std::fprintf(stderr, "[sw] bounded phase from length %llu: %llu levels left, |F|=%u |B|=%u, "
@@ -577,13 +723,29 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       break;
     }
     if (E.F.count == 0 || E.B.count == 0) break;  // a side died out: no reset word within reach
+    if (bounded) break;
+  }
+  std::vector<uint32_t> bounded_tail;
+  if (bounded && !found) {
+    BoundedSearch S{E, A, W, n, k, budget, row_bytes, std::max<u64>(cfg.dfs_min_list_size, 1), max_rt, 0, {}, 0,
+                    {}, {}, st};
+    S.levels.push_back(nullptr);
+    S.explore(0, 0, E.B.count, rt);
+    if (S.best) {
+      found = true;
+      rt = S.best;
+      wit_s = S.best_f;
+      bounded_tail = S.best_tail;
+    } else {
+      rt = max_rt;  // every length up to the bound minus one is excluded
+    }
   }
   if (found) {
     // word = forward letters (depth 1..df) then backward letters (depth db..1)
     std::vector<uint32_t> fw = E.trace(E.F, wit_s, nullptr);
     std::reverse(fw.begin(), fw.end());
     u32 seed_idx = 0;
-    std::vector<uint32_t> bw = E.trace(E.B, wit_q, &seed_idx);
+    std::vector<uint32_t> bw = bounded_tail.empty() ? E.trace(E.B, wit_q, &seed_idx) : bounded_tail;
     std::vector<uint32_t> word = fw;
     word.insert(word.end(), bw.begin(), bw.end());
     std::vector<uint32_t> img = apply_word(A, word);

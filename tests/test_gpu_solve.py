@@ -132,6 +132,22 @@ def test_single_state(ctx):
     assert (r.lower, r.upper) == (0, 0)
 
 
+@pytest.mark.parametrize("seed", [1, 4, 7])
+def test_bounded_phase_in_chunks_under_a_small_budget(ctx, seed):
+    # A 6 MB device budget forces the memory-bounded inverse phase early and
+    # its levels to be taken in chunks of 512 parents (depth-first): the length
+    # must still be exact and the word valid.
+    n, k = 200, 2
+    d = random_dfa(n, k, seed)
+    plan = json.loads(BEAM_EXACT)
+    plan["algorithms"][1]["config"].update({"max_memory_mb": 6, "dfs_min_list_size": 512})
+    r = ctx.solve(d, n, k, json.dumps(plan))
+    ref = oracle.exact(d, n, k, oracle.ExactParams(threads=4))
+    assert (r.lower, r.upper) == (ref.upper, ref.upper)
+    check_word(d, n, k, r)
+    assert r.stats["dfs_sets"] > 0
+
+
 def test_solve_batch_concurrent_streams(ctx):
     autos = [(48, 2, random_dfa(48, 2, 900 + i)) for i in range(12)] + \
             [(100, 3, random_dfa(100, 3, 950 + i)) for i in range(4)] + [(28, 2, cerny(28))]
