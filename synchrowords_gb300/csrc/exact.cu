@@ -697,15 +697,16 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       for (u64 i = 1; i <= R && fits; ++i) {
         const double children = lvl * k;
         total += children * per_row;
-        grow *= 1.6;
+        grow *= 1.35;  // both sides alternate: each side grows ~1.7x every other step
         mitm += t_iter_last * grow;
         // children rows + their sorted copy + the kept level, keys and payloads
         if (children * (3.0 * row_bytes + 32) + (lvl + (double)E.F.count) * row_bytes > (double)budget)
           fits = false;
         lvl *= b_growth;
       }
-      (void)fits;  // over-budget levels are taken in chunks (BoundedSearch)
-      if (total < mitm) {
+      // voluntary switch only when every projected level fits; chunking is the
+      // safety net for an exhausted budget, not a plan
+      if (fits && total < mitm) {
         bounded = true;
         if (E.verbose)
           std::fprintf(stderr, "[sw] bounded phase from length %llu: %llu levels left, |F|=%u |B|=%u, "
