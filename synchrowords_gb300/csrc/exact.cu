@@ -48,9 +48,13 @@ struct Side {
   std::vector<std::unique_ptr<Layer>> layers;
   std::vector<u64> seed_states;  // backward side: the state of each seed row
   double unique_growth = 0;      // distinct children per parent at the last step
+  KeyMap keymap;                 // sort key of this side's layers and visited list
+  bool keymap_chosen = false;
   void reset() {
     count = vis_count = 0;
     unique_growth = 0;
+    keymap = KeyMap{};
+    keymap_chosen = false;
     layers.clear();
     seed_states.clear();
   }
@@ -145,12 +149,12 @@ class Engine {
   DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt, sorted_rows;
 
   // Sort m rows in place by layer key (word 0, then a mix of the other words).
-  void sort_by_layer_key(int W, u64* rows, u32 m) {
+  void sort_by_layer_key(int W, u64* rows, u32 m, const KeyMap& map = KeyMap{}) {
     if (m < 2) return;
     keys.reserve(sizeof(u64) * 2 * m);
     ch_vals.reserve(sizeof(u32) * m);
     sorted_rows.reserve(sizeof(u64) * W * m);
-    launch_layer_keys(W, rows, m, keys.as<u64>(), stream);
+    launch_layer_keys(W, rows, m, keys.as<u64>(), stream, map);
     launch_iota(ch_vals.as<u32>(), m, stream);
     sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), m);
     launch_gather_rows(W, rows, ch_vals.as<u32>(), m, sorted_rows.as<u64>(), stream);
@@ -288,7 +292,7 @@ class Engine {
     // sort the children by layer key (2 words), then gather the rows in that order
     keys.reserve(sizeof(u64) * 2 * N);
     sorted_rows.reserve(sizeof(u64) * W * N);
-    launch_layer_keys(W, ch_rows.as<u64>(), Nc, keys.as<u64>(), stream);
+    launch_layer_keys(W, ch_rows.as<u64>(), Nc, keys.as<u64>(), stream, X.keymap);
     sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
     launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
     launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
@@ -364,13 +368,40 @@ class Engine {
     // visited := visited ∪ layer (both sorted, disjoint)
     X.vis_alt.reserve(sizeof(u64) * W * ((size_t)X.vis_count + f + 1));
     timed(3, (double)(X.vis_count + f) * 8.0 * W * 2, [&] {
-      launch_merge_key(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream);
+      launch_merge_key(W, X.vis.as<u64>(), X.vis_count, X.rows.as<u64>(), f, X.vis_alt.as<u64>(), stream,
+                       X.keymap);
     });
     count_launch();
     std::swap(X.vis.p, X.vis_alt.p);
     std::swap(X.vis.cap, X.vis_alt.cap);
     X.vis_count += f;
     build_tree(W, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split);
+    if (!X.keymap_chosen && X.count >= 2048) choose_keymap(X, W, n);
+  }
+
+  // Once a side's layers are large enough to matter, lead its sort key with
+  // the 64 states most frequent in its current layer (for the backward side
+  // these are states of the complements), and re-sort its visited list.
+  DevBuf d_counts;
+  void choose_keymap(Side& X, int W, int n) {
+    X.keymap_chosen = true;
+    if (n <= 64) return;  // the identity map already covers every state
+    d_counts.reserve(sizeof(u32) * 64 * W);
+    SW_CUDA(cudaMemsetAsync(d_counts.p, 0, sizeof(u32) * 64 * W, stream));
+    launch_state_counts(W, X.rows.as<u64>(), X.count, d_counts.as<u32>(), stream);
+    std::vector<u32> cnt(64 * W);
+    SW_CUDA(cudaMemcpyAsync(cnt.data(), d_counts.p, sizeof(u32) * cnt.size(), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaStreamSynchronize(stream));
+    std::vector<int> idx(n);
+    std::iota(idx.begin(), idx.end(), 0);
+    // column q of the device row holds state q (word q/64, bit 63 - q%64)
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+    KeyMap km;
+    km.identity = 0;
+    for (int j = 0; j < 64; ++j) km.q[j] = (uint16_t)idx[j];
+    X.keymap = km;
+    sort_by_layer_key(W, X.vis.as<u64>(), X.vis_count, X.keymap);
+    count_launch(2);
   }
 
   // Bounded phase helpers.  expand_dedup: preimages (complement rows) of m

@@ -935,57 +935,77 @@ void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, c
 }
 
 // ===========================================================================
-// Layer keys: (word 0, 32-bit mix of words 1..W-1).  Sorting by this key
-// groups sets by their most frequent states (word 0) and makes equal sets
-// adjacent; distinct sets with equal keys are possible only through a hash
-// collision, which can at worst leave a duplicate in a layer (harmless).
+// Layer keys: (64 chosen states packed into one word, 32-bit mix of the row).
+// Sorting by this key groups sets by the pattern of their side's most
+// frequent states and makes equal sets adjacent; distinct sets with equal
+// keys are possible only through a hash collision, which can at worst leave a
+// duplicate in a layer (harmless).  With the identity map the first word is
+// the row's word 0 (states 0..63).
 // ===========================================================================
 template <int W>
-__device__ __forceinline__ u64 rest_mix(const u64* r) {
+__device__ __forceinline__ u64 row_mix(const u64* r, int from) {
   u64 h = 0x9E3779B97F4A7C15ULL;
 #pragma unroll
-  for (int w = 1; w < W; ++w) {
-    u64 x = r[w] ^ (h + 0x632BE59BD9B4E019ULL * (u64)w);
+  for (int w = 0; w < W; ++w) {
+    if (w < from) continue;
+    u64 x = r[w] ^ (h + 0x632BE59BD9B4E019ULL * (u64)(w + 1));
     x ^= x >> 31;
     x *= 0x94D049BB133111EBULL;
     x ^= x >> 29;
     h = (h ^ x) * 0xBF58476D1CE4E5B9ULL;
   }
-  return W > 1 ? (h ^ (h >> 32)) << 32 : 0ULL;
+  return (h ^ (h >> 32)) << 32;
 }
 
 template <int W>
-__global__ void k_layer_keys(const u64* __restrict__ rows, u32 m, u64* __restrict__ keys) {
-  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  u64 r[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) r[w] = rows[(size_t)i * W + w];
-  keys[2 * (size_t)i] = r[0];
-  keys[2 * (size_t)i + 1] = rest_mix<W>(r);
+__device__ __forceinline__ void layer_key(const u64* r, const KeyMap& map, u64& k0, u64& k1) {
+  if (map.identity) {
+    k0 = r[0];
+    k1 = W > 1 ? row_mix<W>(r, 1) : 0ULL;
+    return;
+  }
+  u64 a = 0;
+#pragma unroll 8
+  for (int j = 0; j < 64; ++j) {
+    const int q = map.q[j];
+    a |= ((r[q >> 6] >> (63 - (q & 63))) & 1ULL) << (63 - j);
+  }
+  k0 = a;
+  k1 = row_mix<W>(r, 0);
 }
 
-void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s) {
+template <int W>
+__global__ void k_layer_keys(const u64* __restrict__ rows, u32 m, KeyMap map, u64* __restrict__ keys) {
+  u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  u64 k0, k1;
+  layer_key<W>(rows + (size_t)i * W, map, k0, k1);
+  keys[2 * (size_t)i] = k0;
+  keys[2 * (size_t)i + 1] = k1;
+}
+
+void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s, const KeyMap& map) {
   if (!m) return;
-  SW_DISPATCH_W(W, (k_layer_keys<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, keys)));
+  SW_DISPATCH_W(W, (k_layer_keys<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, map, keys)));
   SW_LAUNCH_CHECK();
 }
 
 // Merge of two arrays sorted by layer key (A first on equal keys).
 template <int W>
-__global__ void k_merge_key(const u64* __restrict__ A, u32 na, const u64* __restrict__ B, u32 nb,
+__global__ void k_merge_key(const u64* __restrict__ A, u32 na, const u64* __restrict__ B, u32 nb, KeyMap map,
                             u64* __restrict__ out) {
   const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= na + nb) return;
   const bool fromA = i < na;
   const u64* x = fromA ? A + (size_t)i * W : B + (size_t)(i - na) * W;
-  const u64 x0 = x[0], x1 = rest_mix<W>(x);
+  u64 x0, x1;
+  layer_key<W>(x, map, x0, x1);
   const u64* other = fromA ? B : A;
   u32 lo = 0, hi = fromA ? nb : na;
   while (lo < hi) {
     const u32 mid = (lo + hi) >> 1;
-    const u64* y = other + (size_t)mid * W;
-    const u64 y0 = y[0], y1 = rest_mix<W>(y);
+    u64 y0, y1;
+    layer_key<W>(other + (size_t)mid * W, map, y0, y1);
     // A element: count B keys strictly less; B element: count A keys <= its key
     const bool before = fromA ? (y0 < x0 || (y0 == x0 && y1 < x1)) : (y0 < x0 || (y0 == x0 && y1 <= x1));
     if (before) lo = mid + 1;
@@ -996,9 +1016,39 @@ __global__ void k_merge_key(const u64* __restrict__ A, u32 na, const u64* __rest
   for (int w = 0; w < W; ++w) out[pos * W + w] = x[w];
 }
 
-void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s) {
+void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s,
+                      const KeyMap& map) {
   if (na + nb == 0) return;
-  SW_DISPATCH_W(W, (k_merge_key<WW><<<(na + nb + 255) / 256, 256, 0, s>>>(A, na, B, nb, out)));
+  SW_DISPATCH_W(W, (k_merge_key<WW><<<(na + nb + 255) / 256, 256, 0, s>>>(A, na, B, nb, map, out)));
+  SW_LAUNCH_CHECK();
+}
+
+// counts[q] += number of rows containing state q (block histograms in shared memory).
+template <int W>
+__global__ void k_state_counts(const u64* __restrict__ rows, u32 m, u32* __restrict__ counts) {
+  __shared__ u32 h[W * 64];
+  for (int i = threadIdx.x; i < W * 64; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int w = 0; w < W; ++w) {
+      u64 v = rows[(size_t)i * W + w];
+      while (v) {
+        const int b = __clzll(v);
+        atomicAdd(&h[w * 64 + b], 1u);
+        v &= ~(1ULL << (63 - b));
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < W * 64; i += blockDim.x)
+    if (h[i]) atomicAdd(&counts[i], h[i]);
+}
+
+void launch_state_counts(int W, const u64* rows, u32 m, u32* counts, cudaStream_t s) {
+  if (!m) return;
+  const u32 blocks = std::min<u32>((m + 255) / 256, (u32)sm_count() * 2);
+  SW_DISPATCH_W(W, (k_state_counts<WW><<<blocks, 256, 0, s>>>(rows, m, counts)));
   SW_LAUNCH_CHECK();
 }
 

@@ -92,11 +92,22 @@ void launch_popcount(int W, const u64* rows, u32 m, u32* out, cudaStream_t s);
 // flags[i] = AND/OR combine: out[i] = (a[i] == 0 && b[i] == 0).
 void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t s);
 
-// Layer keys keys[2i..2i+1] = (word 0 of row i, 32-bit mix of its other
-// words in the high half): sort order of a layer and of the visited list.
-void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s);
-// Merge of two row arrays sorted by layer key.
-void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);
+// Sort key of a side: the 64 states whose pattern leads the key (identity =
+// states 0..63, i.e. word 0 of the row).
+struct KeyMap {
+  uint16_t q[64];
+  int identity = 1;
+};
+
+// Layer keys keys[2i..2i+1] = (the map's 64 states of row i packed MSB-first,
+// 32-bit mix of the row in the high half): sort order of a layer and of the
+// visited list of one side.
+void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s, const KeyMap& map = KeyMap{});
+// Merge of two row arrays sorted by the same layer key.
+void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s,
+                      const KeyMap& map = KeyMap{});
+// counts[q] += rows containing state q (counts: 64*W entries, caller-zeroed).
+void launch_state_counts(int W, const u64* rows, u32 m, u32* counts, cudaStream_t s);
 
 // p[i] = i.
 void launch_iota(u32* p, u32 m, cudaStream_t s);
