@@ -213,6 +213,9 @@ def run_ours(args, world, rank, local):
     torch.cuda.set_device(local)
     dfas = workload_dfas(args.workload, rank)
     n, k, count, plan, desc = WORKLOADS[args.workload]
+    if args.instances:
+        dfas = dfas[:args.instances]
+        count = len(dfas)
     ctx = sw.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -331,6 +334,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
+    ap.add_argument("--instances", type=int, default=0,
+                    help="solve only the first N DFAs of the workload (profiling runs; 0 = all)")
     args = ap.parse_args()
     world, rank, local = dist_setup()
     if world > 1:

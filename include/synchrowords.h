@@ -48,9 +48,9 @@ extern "C" {
 typedef enum {
   SW_ALGO_EXACT = 1,    /* synchrolib/algorithm/exact/ */
   SW_ALGO_BEAM = 2,     /* synchrolib/algorithm/beam/ */
-  SW_ALGO_BRUTE = 3,    /* synchrolib/algorithm/brute/ (outside this library's scope) */
-  SW_ALGO_EPPSTEIN = 4, /* synchrolib/algorithm/eppstein/ (outside this library's scope) */
-  SW_ALGO_REDUCE = 5    /* synchrolib/algorithm/reduce/ (outside this library's scope) */
+  SW_ALGO_BRUTE = 3,    /* synchrolib/algorithm/brute/ */
+  SW_ALGO_EPPSTEIN = 4, /* synchrolib/algorithm/eppstein/ */
+  SW_ALGO_REDUCE = 5    /* synchrolib/algorithm/reduce/ */
 } sw_algo_kind;
 
 /* Evaluated Exact defines (synchrolib/algorithm/exact/config.hpp:24-46). */
@@ -74,11 +74,32 @@ typedef struct {
   int32_t presort_indeg;   /* "presort": 0 = "none", 1 = "indeg" */
 } sw_beam_config;
 
+/* Evaluated Brute defines (synchrolib/algorithm/brute/config.hpp:23-27). */
+typedef struct {
+  uint64_t max_n; /* "max_n" (default 20; above 32 the algorithm refuses to run) */
+} sw_brute_config;
+
+/* Evaluated Eppstein defines (synchrolib/algorithm/eppstein/config.hpp:23-31).
+ * Neither changes the bound; the word is returned whenever it is verified. */
+typedef struct {
+  int32_t transition_tables; /* "transition_tables" (default false) */
+  int32_t find_word;         /* "find_word" (default false) */
+} sw_eppstein_config;
+
+/* Evaluated Reduce defines (synchrolib/algorithm/reduce/config.hpp:24-32). */
+typedef struct {
+  uint64_t min_n;               /* "min_n" (default 80) */
+  uint64_t list_size_threshold; /* "list_size_threshold" (default AUT_N * 16) */
+} sw_reduce_config;
+
 typedef struct {
   int32_t kind; /* sw_algo_kind */
   char name[SW_NAME_LEN];
   sw_exact_config exact;
   sw_beam_config beam;
+  sw_brute_config brute;
+  sw_eppstein_config eppstein;
+  sw_reduce_config reduce;
 } sw_algorithm;
 
 /* Global plan keys (app/jit.hpp:112-141, docs/config.md:15-27). */
@@ -108,6 +129,8 @@ typedef struct {
   uint64_t dfs_sets;          /* sets generated in the memory-bounded inverse DFS phase */
   uint64_t kernel_launches;   /* device kernels launched by the solve */
   double device_ms;           /* wall time of the solve spent in the GPU search */
+  uint64_t reduce_bfs_steps;  /* BFS steps of a successful Reduce (0 if none) */
+  uint64_t reduced_states;    /* states left after a successful Reduce (0 if none) */
 } sw_stats;
 
 typedef struct {

@@ -77,6 +77,9 @@ def lib():
                                      ctypes.POINTER(_BeamParams), ctypes.POINTER(_Bounds)]
         _lib.oracle_brute.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.POINTER(ctypes.c_int64)]
+        _lib.oracle_eppstein.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32, ctypes.c_uint32,
+                                         ctypes.POINTER(_Bounds), ctypes.POINTER(ctypes.c_uint32),
+                                         ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
     return _lib
 
 
@@ -167,6 +170,21 @@ def brute(delta: Sequence[int], n: int, k: int) -> int:
     if rc != 0:
         raise RuntimeError(f"oracle_brute failed with {rc}")
     return out.value
+
+
+def eppstein(delta: Sequence[int], n: int, k: int, lower: int = 0, upper: Optional[int] = None):
+    """Eppstein's greedy upper bound: (Result, word) — word None when the bound is unchanged."""
+    b = _Bounds(0, lower, default_upper_bound(n) if upper is None else upper)
+    before = b.upper
+    cap = n * n * n // 6 + n + 1
+    buf = (ctypes.c_uint32 * cap)()
+    wl = ctypes.c_uint64()
+    rc = lib().oracle_eppstein(_arr(delta), n, k, ctypes.byref(b), buf, cap, ctypes.byref(wl))
+    if rc != 0:
+        raise RuntimeError(f"oracle_eppstein failed with {rc}")
+    res = Result(b.lower, b.upper, bool(b.non_synchro))
+    word = list(buf[:wl.value]) if (wl.value or b.upper != before) and not b.non_synchro else None
+    return res, word
 
 
 def apply_word(delta: Sequence[int], n: int, k: int, word: Sequence[int]) -> set:

@@ -1375,4 +1375,83 @@ int oracle_brute(const uint32_t* delta, uint32_t n, uint32_t k, int64_t* out) {
   return 0;
 }
 
+// Eppstein's greedy bound (eppstein.hpp:82-114) over the pairs tree
+// (pairs_tree.hpp:25-62), restated sequentially with the reference's FIFO
+// queue so that every pair records the same first letter.  `r` in/out as
+// AlgoResult; word (capacity word_cap) receives the greedy word.
+// Returns 0, or -1 on bad arguments; *word_len = letters written.
+int oracle_eppstein(const uint32_t* delta, uint32_t n, uint32_t k, oracle_bounds* r, uint32_t* word,
+                    uint64_t word_cap, uint64_t* word_len) {
+  if (!delta || !r || n == 0 || k == 0 || n > 512) return -1;
+  for (size_t i = 0; i < (size_t)n * k; ++i)
+    if (delta[i] >= n) return -1;
+  if (word_len) *word_len = 0;
+  if (r->non_synchro || r->lower == r->upper) return 0;  // eppstein.hpp:28-34
+  orc::Aut A{n, k, std::vector<uint32_t>(delta, delta + (size_t)n * k)};
+  orc::InvAut inv(A);
+  const size_t N = n;
+  std::vector<uint32_t> len(N * N, 0), let(N * N, 0);
+  std::vector<std::pair<uint32_t, uint32_t>> queue;
+  queue.reserve(N * (N - 1) / 2);
+  for (uint32_t t = 0; t < n; ++t)
+    for (uint32_t a = 0; a < k; ++a)
+      for (uint32_t i1 = inv.begin[a * n + t]; i1 < inv.end[a * n + t]; ++i1)
+        for (uint32_t i2 = i1 + 1; i2 < inv.end[a * n + t]; ++i2) {
+          const uint32_t p = inv.edges[a * n + i1], q = inv.edges[a * n + i2];
+          if (len[p * N + q]) continue;
+          len[p * N + q] = len[q * N + p] = 1;
+          let[p * N + q] = let[q * N + p] = a;
+          queue.push_back({p, q});
+        }
+  for (size_t head = 0; head < queue.size() && queue.size() < N * (N - 1) / 2; ++head) {
+    const uint32_t v1 = queue[head].first, v2 = queue[head].second;
+    const uint32_t l = len[v1 * N + v2] + 1;
+    for (uint32_t a = 0; a < k; ++a)
+      for (uint32_t i1 = inv.begin[a * n + v1]; i1 < inv.end[a * n + v1]; ++i1)
+        for (uint32_t i2 = inv.begin[a * n + v2]; i2 < inv.end[a * n + v2]; ++i2) {
+          const uint32_t p = inv.edges[a * n + i1], q = inv.edges[a * n + i2];
+          if (len[p * N + q]) continue;
+          len[p * N + q] = len[q * N + p] = l;
+          let[p * N + q] = let[q * N + p] = a;
+          queue.push_back({p, q});
+        }
+  }
+  if (queue.size() < N * (N - 1) / 2) {  // pairs_tree.hpp:95-100
+    r->non_synchro = 1;
+    return 0;
+  }
+  std::vector<char> cur(n, 1), nxt(n);
+  uint64_t total = 0, wl = 0;
+  size_t size = n;
+  do {
+    uint32_t p = 0, q = 0, l = n * n;
+    for (uint32_t v1 = 0; v1 + 1 < n; ++v1)
+      if (cur[v1])
+        for (uint32_t v2 = v1 + 1; v2 < n; ++v2)
+          if (cur[v2] && len[v1 * N + v2] < l) {
+            p = v1;
+            q = v2;
+            l = len[v1 * N + v2];
+          }
+    total += l;
+    if (total > r->upper) return 0;  // bound unchanged (eppstein.hpp:104-106)
+    while (p != q) {
+      const uint32_t a = let[p * N + q];
+      if (word && wl < word_cap) word[wl] = a;
+      ++wl;
+      std::fill(nxt.begin(), nxt.end(), 0);
+      for (uint32_t s = 0; s < n; ++s)
+        if (cur[s]) nxt[A.at(s, a)] = 1;
+      cur.swap(nxt);
+      p = A.at(p, a);
+      q = A.at(q, a);
+    }
+    size = 0;
+    for (uint32_t s = 0; s < n; ++s) size += cur[s];
+  } while (size > 1);
+  r->upper = total;
+  if (word_len) *word_len = wl;
+  return 0;
+}
+
 }  // extern "C"

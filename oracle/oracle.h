@@ -64,6 +64,9 @@ int oracle_exact(const uint32_t* delta, uint32_t n, uint32_t k, const oracle_exa
 int oracle_beam(const uint32_t* delta, uint32_t n, uint32_t k, const oracle_beam_params* p,
                 oracle_bounds* r);
 int oracle_brute(const uint32_t* delta, uint32_t n, uint32_t k, int64_t* out);
+/* Eppstein greedy bound (eppstein.hpp:82-114); `r` in/out, word optional. */
+int oracle_eppstein(const uint32_t* delta, uint32_t n, uint32_t k, oracle_bounds* r, uint32_t* word,
+                    uint64_t word_cap, uint64_t* word_len);
 
 #ifdef __cplusplus
 }

@@ -51,9 +51,21 @@ class _BeamCfg(ctypes.Structure):
                 ("max_iter", ctypes.c_int64), ("presort_indeg", ctypes.c_int32)]
 
 
+class _BruteCfg(ctypes.Structure):
+    _fields_ = [("max_n", ctypes.c_uint64)]
+
+
+class _EppsteinCfg(ctypes.Structure):
+    _fields_ = [("transition_tables", ctypes.c_int32), ("find_word", ctypes.c_int32)]
+
+
+class _ReduceCfg(ctypes.Structure):
+    _fields_ = [("min_n", ctypes.c_uint64), ("list_size_threshold", ctypes.c_uint64)]
+
+
 class _Algo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("name", ctypes.c_char * NAME_LEN), ("exact", _ExactCfg),
-                ("beam", _BeamCfg)]
+                ("beam", _BeamCfg), ("brute", _BruteCfg), ("eppstein", _EppsteinCfg), ("reduce", _ReduceCfg)]
 
 
 class _Plan(ctypes.Structure):
@@ -70,7 +82,8 @@ class _Stats(ctypes.Structure):
     _fields_ = [("subsets_expanded", ctypes.c_uint64), ("subsets_kept", ctypes.c_uint64),
                 ("trie_queries", ctypes.c_uint64), ("logical_pairs", ctypes.c_uint64),
                 ("meet_pairs", ctypes.c_uint64), ("bfs_steps", ctypes.c_uint64), ("ibfs_steps", ctypes.c_uint64),
-                ("dfs_sets", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("device_ms", ctypes.c_double)]
+                ("dfs_sets", ctypes.c_uint64), ("kernel_launches", ctypes.c_uint64), ("device_ms", ctypes.c_double), ("reduce_bfs_steps", ctypes.c_uint64),
+                ("reduced_states", ctypes.c_uint64)]
 
 
 class _Result(ctypes.Structure):
@@ -160,6 +173,12 @@ def plan_from_json(text: str, n: int, k: int) -> dict:
             d.update({f: getattr(a.exact, f) for f, _ in _ExactCfg._fields_})
         elif a.kind == 2:
             d.update({f: getattr(a.beam, f) for f, _ in _BeamCfg._fields_})
+        elif a.kind == 3:
+            d.update({f: getattr(a.brute, f) for f, _ in _BruteCfg._fields_})
+        elif a.kind == 4:
+            d.update({f: getattr(a.eppstein, f) for f, _ in _EppsteinCfg._fields_})
+        elif a.kind == 5:
+            d.update({f: getattr(a.reduce, f) for f, _ in _ReduceCfg._fields_})
         algos.append(d)
     return {"upper_bound": p.upper_bound, "threads": p.threads, "gpu": p.gpu,
             "gpu_max_memory_mb": p.gpu_max_memory_mb, "algorithms": algos}

@@ -128,19 +128,43 @@ int run_plan(sw::Solver& solver, const uint32_t* delta, uint32_t n, uint32_t k, 
     err = "too many algorithms";
     return SW_ERR_CONFIG;
   }
+  // After a successful Reduce the remaining algorithms see the reduced
+  // automaton (app/main.cpp:60-68, jit/jitmain.cpp:21-45); only Exact can use
+  // it, the others refuse and leave the bounds alone (beam.hpp:48-52,
+  // brute.hpp:38-42, eppstein.hpp:38-42, reduce.hpp:34-38).
+  sw::ReduceState red;
   for (uint32_t i = 0; i < plan->n_algorithms; ++i) {
     const sw_algorithm& alg = plan->algorithms[i];
     auto t0 = std::chrono::steady_clock::now();
-    switch (alg.kind) {
-      case SW_ALGO_EXACT:
-        solver.exact(A, alg.exact, b, r->stats);
-        break;
-      case SW_ALGO_BEAM:
-        solver.beam(A, alg.beam, b, r->stats);
-        break;
-      default:
-        err = std::string("algorithm ") + alg.name + " is outside this library's scope (supported: Exact, Beam)";
+    if (red.active && alg.kind != SW_ALGO_EXACT) {
+      if (alg.kind < SW_ALGO_EXACT || alg.kind > SW_ALGO_REDUCE) {
+        err = std::string("algorithm ") + alg.name + " is outside this library's scope";
         return SW_ERR_UNSUPPORTED;
+      }
+    } else {
+      switch (alg.kind) {
+        case SW_ALGO_EXACT:
+          if (red.active)
+            solver.exact(red.reduced, alg.exact, b, r->stats, &red);
+          else
+            solver.exact(A, alg.exact, b, r->stats);
+          break;
+        case SW_ALGO_BEAM:
+          solver.beam(A, alg.beam, b, r->stats);
+          break;
+        case SW_ALGO_EPPSTEIN:
+          solver.eppstein(A, alg.eppstein, b, r->stats);
+          break;
+        case SW_ALGO_BRUTE:
+          solver.brute(A, alg.brute, b, r->stats);
+          break;
+        case SW_ALGO_REDUCE:
+          solver.reduce(A, alg.reduce, b, r->stats, red);
+          break;
+        default:
+          err = std::string("algorithm ") + alg.name + " is outside this library's scope";
+          return SW_ERR_UNSUPPORTED;
+      }
     }
     auto ms = std::chrono::duration_cast<std::chrono::milliseconds>(std::chrono::steady_clock::now() - t0).count();
     set_name(r->runs[r->n_runs].name, alg.name);

@@ -1,0 +1,48 @@
+// Device parts of the reference's small algorithms: the Eppstein greedy upper
+// bound (pairs.cu) and the power-set BFS `Brute` (brute.cu).  Launchers are
+// asynchronous on the given stream; scratch comes from the caller.
+#pragma once
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace sw {
+
+// ---- Eppstein (synchrolib/algorithm/eppstein/eppstein.hpp:82-114 over the
+// pairs tree of synchrolib/data_structures/pairs_tree.hpp:25-62) ----------
+
+// Result words written by launch_eppstein into `out` (u32[8]).
+enum EppsteinStatus : u32 {
+  kEppFound = 0,       // out[1..2] = length (lo, hi), out[3] = letters written
+  kEppOverBound = 1,   // the greedy word grew past `upper` (eppstein.hpp:104-106)
+  kEppNonSynchro = 2,  // some pair never reaches the diagonal (pairs_tree.hpp:95-100)
+  kEppWordCapacity = 3,
+};
+
+size_t eppstein_scratch_bytes(int n);
+
+// One block: breadth-first pair tree (per pair {p, q} the length of the
+// shortest word merging it and that word's first letter, the same first
+// letter the reference's queue order records), then the greedy walk that
+// repeatedly merges the closest pair of the current image.  Letters go to
+// `word` (capacity `word_cap`).
+void launch_eppstein(const TransTables& t, u64 upper, void* scratch, u32* out, uint8_t* word, u64 word_cap,
+                     cudaStream_t s);
+
+// ---- Brute (synchrolib/algorithm/brute/brute.hpp:88-122), n <= 32 --------
+
+// Bitmap of visited subsets: 2^n bits.
+size_t brute_visited_bytes(int n);
+
+// One BFS level: every image of every frontier mask under every letter that
+// was not visited yet is marked and appended to `next` (next_count[0] counts,
+// capped at next_cap: the excess is counted but not stored).  found[0] = 1 and
+// found[1] = the mask when a singleton is produced.
+void launch_brute_level(const uint16_t* delta, int n, int k, const u32* frontier, u32 count, u32* visited,
+                        u32* next, u32 next_cap, u32* next_count, u32* found, cudaStream_t s);
+
+// Word back-tracking: best[0] = min over (i, a) with image(level[i], a) ==
+// target of i * k + a (caller initialises best[0] to ~0).
+void launch_brute_parent(const uint16_t* delta, int n, int k, const u32* level, u32 count, u32 target, u64* best,
+                         cudaStream_t s);
+
+}  // namespace sw

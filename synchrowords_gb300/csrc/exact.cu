@@ -25,6 +25,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "algos.cuh"
 #include "exact.hpp"
 #include "kernels.cuh"
 
@@ -146,6 +147,7 @@ class Engine {
   TransTables tables;
   // scratch
   DevBuf ch_rows, ch_vals, alt_rows, alt_vals, uq_rows, uq_vals, new_vals;
+  DevBuf epp_scratch, epp_word, br_visited, br_arena;
   DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt, sorted_rows;
 
   // Sort m rows in place by layer key (word 0, then a mix of the other words).
@@ -379,13 +381,18 @@ class Engine {
     if (!X.keymap_chosen && X.count >= 2048) choose_keymap(X, W, n);
   }
 
-  // Once a side's layers are large enough to matter, lead its sort key with
-  // the 64 states most frequent in its current layer (for the backward side
-  // these are states of the complements), and re-sort its visited list.
+  // Optionally, once a side's layers are large enough to matter, lead its
+  // sort key with 64 chosen states of its current layer (for the backward
+  // side, states of the complements) and re-sort its visited list.
   DevBuf d_counts;
   void choose_keymap(Side& X, int W, int n) {
     X.keymap_chosen = true;
     if (n <= 64) return;  // the identity map already covers every state
+    // Measured on random binary DFAs (n = 200 and 320), re-keying made the
+    // subset checks slower than the identity key, so it is opt-in:
+    // SW_SORT_KEY=frequent or SW_SORT_KEY=balanced.
+    static const char* opt = std::getenv("SW_SORT_KEY");
+    if (!opt || (std::string(opt) != "frequent" && std::string(opt) != "balanced")) return;
     d_counts.reserve(sizeof(u32) * 64 * W);
     SW_CUDA(cudaMemsetAsync(d_counts.p, 0, sizeof(u32) * 64 * W, stream));
     launch_state_counts(W, X.rows.as<u64>(), X.count, d_counts.as<u32>(), stream);
@@ -394,8 +401,16 @@ class Engine {
     SW_CUDA(cudaStreamSynchronize(stream));
     std::vector<int> idx(n);
     std::iota(idx.begin(), idx.end(), 0);
-    // column q of the device row holds state q (word q/64, bit 63 - q%64)
-    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+    // column q of the device row holds state q (word q/64, bit 63 - q%64).
+    // "balanced" leads with the states closest to half the layer (the most
+    // even splits), "frequent" with the most frequent.
+    if (std::string(opt) == "balanced") {
+      const long long half = X.count / 2;
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int a, int b) { return std::llabs(cnt[a] - half) < std::llabs(cnt[b] - half); });
+    } else {
+      std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+    }
     KeyMap km;
     km.identity = 0;
     for (int j = 0; j < 64; ++j) km.q[j] = (uint16_t)idx[j];
@@ -595,8 +610,10 @@ static std::vector<uint32_t> image_frequency_order(const Automaton& A) {
   return order;
 }
 
-void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, sw_stats& st) {
-  const Automaton A = permute(A0, image_frequency_order(A0));
+void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, sw_stats& st,
+                   const ReduceState* red) {
+  const std::vector<uint32_t> order = image_frequency_order(A0);
+  const Automaton A = permute(A0, order);
   if (b.non_synchro || b.lower == b.upper) return;  // exact.cpp:45-47
   if (A.n == 1) {                                   // exact.cpp:49-53
     b.lower = b.upper = 0;
@@ -622,9 +639,19 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
   {
     std::vector<u64> full(W, 0);
     for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
-    E.F.rows.reserve(sizeof(u64) * W);
-    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
-    E.F.count = 1;
+    std::vector<u64> fseeds;
+    if (red) {
+      // exact.cpp:130-146: the forward side starts from the reduced BFS list
+      fseeds.assign((size_t)W * red->seeds.size(), 0);
+      for (size_t i = 0; i < red->seeds.size(); ++i)
+        for (uint32_t q : red->seeds[i]) fseeds[i * W + (order[q] >> 6)] |= state_bit((int)order[q]);
+    } else {
+      fseeds = full;
+    }
+    const u32 nf = (u32)(fseeds.size() / W);
+    E.F.rows.reserve(sizeof(u64) * W * std::max<u32>(nf, 1));
+    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, fseeds.data(), sizeof(u64) * W * nf, cudaMemcpyHostToDevice, E.stream));
+    E.F.count = nf;
     std::vector<uint32_t> seeds = backward_seeds(A);
     std::vector<u64> rows((size_t)W * std::max<size_t>(seeds.size(), 1), 0);
     for (size_t i = 0; i < seeds.size(); ++i) {
@@ -641,7 +668,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     E.F.vis.reserve(sizeof(u64) * W);
     E.B.vis.reserve(sizeof(u64) * W * std::max<size_t>(seeds.size(), 1));
     SW_CUDA(cudaMemcpyAsync(E.F.vis.p, E.F.rows.p, sizeof(u64) * W, cudaMemcpyDeviceToDevice, E.stream));
-    E.F.vis_count = 1;
+    E.F.vis_count = red ? 0 : 1;  // a reduced list starts with an empty visited list, as the reference's does
     if (!seeds.empty()) {
       // seeds are already sorted ascending by state = descending by row value
       // for complements; sort them properly via the row sort.
@@ -772,15 +799,24 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
       rt = max_rt;  // every length up to the bound minus one is excluded
     }
   }
+  if (red) {  // exact.cpp:83-87: lengths count the reduction's BFS steps
+    rt += red->bfs_steps;
+    b.lower += red->bfs_steps;
+    b.upper += red->bfs_steps;
+  }
   if (found) {
-    // word = forward letters (depth 1..df) then backward letters (depth db..1)
-    std::vector<uint32_t> fw = E.trace(E.F, wit_s, nullptr);
+    // word = (reduction prefix) forward letters (depth 1..df) then backward
+    // letters (depth db..1)
+    u32 fseed = 0;
+    std::vector<uint32_t> fw = E.trace(E.F, wit_s, &fseed);
     std::reverse(fw.begin(), fw.end());
     u32 seed_idx = 0;
     std::vector<uint32_t> bw = bounded_tail.empty() ? E.trace(E.B, wit_q, &seed_idx) : bounded_tail;
-    std::vector<uint32_t> word = fw;
+    std::vector<uint32_t> word;
+    if (red) word = red->prefix.at(fseed);
+    word.insert(word.end(), fw.begin(), fw.end());
     word.insert(word.end(), bw.begin(), bw.end());
-    std::vector<uint32_t> img = apply_word(A, word);
+    std::vector<uint32_t> img = apply_word(red ? red->original : A, word);
     if (img.size() != 1 || word.size() != rt)
       throw std::runtime_error("internal error: reconstructed word does not synchronize (length " +
                                std::to_string(word.size()) + ", image " + std::to_string(img.size()) + ")");
@@ -1037,6 +1073,284 @@ uint64_t Solver::sort_unique(uint32_t n, uint64_t* sets, uint64_t count) {
   SW_CUDA(cudaStreamSynchronize(E.stream));
   from_device_rows(rows.data(), u, n, W, sets);
   return u;
+}
+
+// ---------------------------------------------------------------------------
+// Eppstein (synchrolib/algorithm/eppstein/eppstein.hpp:26-76).
+// ---------------------------------------------------------------------------
+void Solver::eppstein(const Automaton& A, const sw_eppstein_config&, Bounds& b, sw_stats& st) {
+  if (b.non_synchro || b.lower == b.upper) return;  // eppstein.hpp:28-34
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  auto t0 = std::chrono::steady_clock::now();
+  E.upload_tables(A);
+  const u64 n = A.n;
+  E.epp_scratch.reserve(eppstein_scratch_bytes((int)n));
+  // the greedy word is at most (n^3 - n) / 6 letters long (Eppstein 1990)
+  const u64 cap = std::min<u64>(b.upper, n * n * n / 6 + n) + 1;
+  E.epp_word.reserve(cap);
+  u32* out = E.d_misc + 16;
+  SW_CUDA(cudaMemsetAsync(out, 0, 8 * sizeof(u32), E.stream));
+  launch_eppstein(E.tables, b.upper, E.epp_scratch.p, out, E.epp_word.as<uint8_t>(), cap, E.stream);
+  ++st.kernel_launches;
+  u32* h = E.pinned.as<u32>();
+  SW_CUDA(cudaMemcpyAsync(h, out, 8 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  const u32 status = h[0];
+  const u64 len = (u64)h[1] | ((u64)h[2] << 32);
+  const u64 letters = h[3];
+  st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (status == kEppNonSynchro) {  // eppstein.hpp:53-57
+    b.non_synchro = true;
+    return;
+  }
+  if (status == kEppOverBound) return;  // eppstein.hpp:60-62: bound unchanged
+  if (status != kEppFound) throw std::runtime_error("internal: Eppstein word buffer too small");
+  const u64 old_upper = b.upper;
+  b.upper = len;
+  if (letters == len) {
+    std::vector<uint8_t> w8(letters);
+    if (letters) SW_CUDA(cudaMemcpy(w8.data(), E.epp_word.p, letters, cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> word(w8.begin(), w8.end());
+    if (apply_word(A, word).size() != 1) throw std::runtime_error("internal: Eppstein word does not synchronize");
+    if (!b.has_word || len < old_upper) {
+      b.has_word = true;
+      b.word = std::move(word);
+    }
+  }
+  if (b.has_word && b.word.size() != b.upper) b.has_word = false;
+}
+
+// ---------------------------------------------------------------------------
+// Brute (synchrolib/algorithm/brute/brute.hpp:28-71).
+// ---------------------------------------------------------------------------
+void Solver::brute(const Automaton& A, const sw_brute_config& cfg, Bounds& b, sw_stats& st) {
+  if (b.non_synchro || b.lower == b.upper) return;  // brute.hpp:30-36
+  if (cfg.max_n > 32) return;                       // brute.hpp:44-47: refused, bounds unchanged
+  if (A.n > cfg.max_n) return;                      // brute.hpp:49-52
+  if (A.n == 1) {
+    b.lower = b.upper = 0;
+    b.has_word = true;
+    b.word.clear();
+    return;
+  }
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  auto t0 = std::chrono::steady_clock::now();
+  E.upload_tables(A);
+  const int n = (int)A.n, k = (int)A.k;
+  const u64 space = 1ULL << n;  // masks; every level holds new masks only, so all levels fit in `space`
+  const u32 full = n == 32 ? 0xffffffffu : ((1u << n) - 1u);
+  E.br_visited.reserve(brute_visited_bytes(n));
+  SW_CUDA(cudaMemsetAsync(E.br_visited.p, 0, brute_visited_bytes(n), E.stream));
+  const u32 full_bit = 1u << (full & 31u);
+  SW_CUDA(cudaMemcpyAsync(E.br_visited.as<u32>() + (full >> 5), &full_bit, sizeof(u32), cudaMemcpyHostToDevice,
+                          E.stream));
+  E.br_arena.reserve(sizeof(u32) * std::min<u64>(space, 1ULL << 20));
+  SW_CUDA(cudaMemcpyAsync(E.br_arena.p, &full, sizeof(u32), cudaMemcpyHostToDevice, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  std::vector<u64> off{0, 1};  // level j = arena[off[j], off[j+1])
+  u32* ctrl = E.d_misc + 24;   // [0] next count, [1] found, [2] singleton
+  u32* h = E.pinned.as<u32>();
+  u64 length = 0;
+  u32 target = 0;
+  for (u64 depth = 0;; ++depth) {
+    const u64 begin = off[depth], end = off[depth + 1], count = end - begin;
+    const u64 room = std::min<u64>(count * (u64)k, space - end);
+    const size_t need = sizeof(u32) * (end + room);
+    if (need > E.br_arena.cap) {  // grow, keeping the stored levels
+      DevBuf bigger;
+      bigger.reserve(std::max(need, 2 * E.br_arena.cap));
+      SW_CUDA(cudaMemcpyAsync(bigger.p, E.br_arena.p, sizeof(u32) * end, cudaMemcpyDeviceToDevice, E.stream));
+      SW_CUDA(cudaStreamSynchronize(E.stream));
+      std::swap(bigger.p, E.br_arena.p);
+      std::swap(bigger.cap, E.br_arena.cap);
+    }
+    u32* arena = E.br_arena.as<u32>();
+    SW_CUDA(cudaMemsetAsync(ctrl, 0, 3 * sizeof(u32), E.stream));
+    launch_brute_level(E.t_delta.as<uint16_t>(), n, k, arena + begin, (u32)count, E.br_visited.as<u32>(), arena + end,
+                       (u32)room, ctrl, ctrl + 1, E.stream);
+    ++st.kernel_launches;
+    SW_CUDA(cudaMemcpyAsync(h, ctrl, 3 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    st.subsets_expanded += count * (u64)k;
+    st.subsets_kept += h[0];
+    if (h[0] > room) throw std::runtime_error("internal: Brute level overflow");
+    if (h[1]) {
+      length = depth + 1;
+      target = h[2];
+      break;
+    }
+    if (h[0] == 0) {  // brute.hpp:61-65: BFS exhausted without a singleton
+      b.non_synchro = true;
+      st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      return;
+    }
+    off.push_back(end + h[0]);
+  }
+  // walk back through the stored levels: a parent of `target` in level j
+  std::vector<uint32_t> word(length);
+  u64* best = reinterpret_cast<u64*>(E.d_misc + 32);
+  for (u64 j = length; j-- > 0;) {
+    const u64 begin = off[j], count = off[j + 1] - begin;
+    SW_CUDA(cudaMemsetAsync(best, 0xff, sizeof(u64), E.stream));
+    launch_brute_parent(E.t_delta.as<uint16_t>(), n, k, E.br_arena.as<u32>() + begin, (u32)count, target, best,
+                        E.stream);
+    ++st.kernel_launches;
+    u64 hb = 0;
+    SW_CUDA(cudaMemcpyAsync(h, best, sizeof(u64), cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    std::memcpy(&hb, h, sizeof(u64));
+    if (hb == ~0ULL) throw std::runtime_error("internal: Brute parent not found");
+    word[j] = (uint32_t)(hb % (u64)k);
+    SW_CUDA(cudaMemcpy(&target, E.br_arena.as<u32>() + begin + hb / (u64)k, sizeof(u32), cudaMemcpyDeviceToHost));
+  }
+  if (apply_word(A, word).size() != 1) throw std::runtime_error("internal: Brute word does not synchronize");
+  b.lower = b.upper = length;  // brute.hpp:66-70
+  b.has_word = true;
+  b.word = std::move(word);
+  st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// ---------------------------------------------------------------------------
+// Reduce (synchrolib/algorithm/reduce/reduce.hpp:31-91).  The BFS steps are
+// the forward side of the exact search (expansion, duplicate removal, the two
+// dominance checks, visited merge); the reachability closure and relabelling
+// of the small final list are host bookkeeping.
+// ---------------------------------------------------------------------------
+void Solver::reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, sw_stats& st, ReduceState& red) {
+  if (b.non_synchro || b.lower == b.upper) return;  // reduce.hpp:40-46
+  if (A.n < cfg.min_n) return;                      // reduce.hpp:48-50
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  E.st = &st;
+  auto t0 = std::chrono::steady_clock::now();
+  const int n = (int)A.n, k = (int)A.k, W = words_for(n);
+  E.upload_tables(A);
+  E.F.reset();
+  std::vector<u64> full(W, 0);
+  for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
+  E.F.rows.reserve(sizeof(u64) * W);
+  SW_CUDA(cudaMemcpyAsync(E.F.rows.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
+  E.F.count = 1;
+  E.F.vis_count = 0;  // reduce.hpp:128: the visited list starts empty
+  const u64 max_mlsw = b.upper - 1;
+  u64 mlsw = 0;
+  bool found = false;
+  std::vector<uint32_t> word;
+  DevBuf counts;
+  auto done = [&] {
+    st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    E.st = nullptr;
+  };
+  // reduce.hpp:96-109 (process_short_bfs) with bfs_step :171-198
+  while (mlsw < max_mlsw) {
+    if (E.F.count > cfg.list_size_threshold) break;
+    mlsw++;
+    st.bfs_steps++;
+    if (E.F.count == 0) continue;  // an exhausted list stays empty up to the bound, as in the reference
+    E.step(E.F, true, W, n, k, true);
+    const u32 m = E.F.count;
+    if (!m) continue;
+    counts.reserve(sizeof(u32) * m);
+    launch_popcount(W, E.F.rows.as<u64>(), m, counts.as<u32>(), E.stream);
+    E.count_launch();
+    std::vector<u32> pc(m);
+    SW_CUDA(cudaMemcpyAsync(pc.data(), counts.p, sizeof(u32) * m, cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    for (u32 i = 0; i < m; ++i)
+      if (pc[i] == 1) {
+        word = E.trace(E.F, i, nullptr);
+        std::reverse(word.begin(), word.end());
+        found = true;
+        break;
+      }
+    if (found) break;
+  }
+  if (!found && mlsw == max_mlsw) {  // reduce.hpp:60-63: every shorter length is excluded
+    mlsw++;
+    if (b.has_word && b.word.size() != mlsw) b.has_word = false;
+    b.lower = b.upper = mlsw;
+    return done();
+  }
+  if (found) {  // reduce.hpp:65-70
+    if (apply_word(A, word).size() != 1 || word.size() != mlsw)
+      throw std::runtime_error("internal: Reduce word does not synchronize");
+    b.lower = b.upper = mlsw;
+    b.has_word = true;
+    b.word = word;
+    return done();
+  }
+  // reduce.hpp:112-143 (try_to_reduce): states reachable from the list
+  const u32 m = E.F.count;
+  std::vector<u64> rows((size_t)m * W);
+  if (m) SW_CUDA(cudaMemcpyAsync(rows.data(), E.F.rows.p, sizeof(u64) * W * m, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  std::vector<char> reach(n, 0);
+  std::vector<uint32_t> stack;
+  for (u32 i = 0; i < m; ++i)
+    for (int q = 0; q < n; ++q)
+      if ((rows[(size_t)i * W + (q >> 6)] & state_bit(q)) && !reach[q]) {
+        reach[q] = 1;
+        stack.push_back((uint32_t)q);
+      }
+  while (!stack.empty()) {  // reduce.hpp:145-169
+    const uint32_t q = stack.back();
+    stack.pop_back();
+    for (int a = 0; a < k; ++a) {
+      const uint32_t p = A.at(q, (uint32_t)a);
+      if (!reach[p]) {
+        reach[p] = 1;
+        stack.push_back(p);
+      }
+    }
+  }
+  uint32_t rn = 0;
+  std::vector<uint32_t> map(n, 0);
+  for (int q = 0; q < n; ++q)
+    if (reach[q]) map[q] = rn++;
+  if (rn == (uint32_t)n || rn == 0) return done();  // reduce.hpp:72-75: skipping reduction
+  red = ReduceState{};
+  red.active = true;
+  red.bfs_steps = mlsw;
+  red.original = A;
+  red.reduced.n = rn;
+  red.reduced.k = A.k;
+  red.reduced.t.assign((size_t)rn * A.k, 0);
+  for (int q = 0; q < n; ++q)
+    if (reach[q])
+      for (uint32_t a = 0; a < A.k; ++a) red.reduced.t[(size_t)map[q] * A.k + a] = map[A.at((uint32_t)q, a)];
+  // each list set and the word that produced it, traced on the host from the
+  // per-layer origin arrays
+  std::vector<std::vector<u32>> origin(E.F.layers.size());
+  for (size_t d = 0; d < E.F.layers.size(); ++d) {
+    const Layer& L = *E.F.layers[d];
+    origin[d].resize(L.count);
+    if (L.count)
+      SW_CUDA(cudaMemcpyAsync(origin[d].data(), L.origin.p, sizeof(u32) * L.count, cudaMemcpyDeviceToHost,
+                              E.stream));
+  }
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  red.seeds.resize(m);
+  red.prefix.resize(m);
+  for (u32 i = 0; i < m; ++i) {
+    for (int q = 0; q < n; ++q)
+      if (rows[(size_t)i * W + (q >> 6)] & state_bit(q)) red.seeds[i].push_back(map[q]);
+    std::vector<uint32_t>& w = red.prefix[i];
+    u32 idx = i;
+    for (size_t d = E.F.layers.size(); d-- > 0;) {
+      const u32 o = origin[d][idx];
+      w.push_back(o / E.F.layers[d]->parent_count);
+      idx = o % E.F.layers[d]->parent_count;
+    }
+    std::reverse(w.begin(), w.end());
+  }
+  st.reduce_bfs_steps = mlsw;
+  st.reduced_states = rn;
+  // reduce.hpp:77-84: the remaining search works on reduced lengths
+  b.lower = b.lower > mlsw ? b.lower - mlsw : 0;
+  b.upper -= mlsw;
+  done();
 }
 
 }  // namespace sw

@@ -21,6 +21,17 @@ struct Bounds {
 
 class Engine;  // device state, defined in exact.cu
 
+// What a successful Reduce hands to the algorithms after it
+// (synchrolib/algorithm/algorithm.hpp:29-34 ReduceData, reduce.hpp:75-90).
+struct ReduceState {
+  bool active = false;    // the automaton was reduced (the reference's reduce->done)
+  uint64_t bfs_steps = 0; // BFS steps the reduction took (added back by Exact)
+  Automaton original;     // the automaton before reduction (words are checked on it)
+  Automaton reduced;      // restriction to the states reachable from the BFS list
+  std::vector<std::vector<uint32_t>> seeds;   // BFS list, as state lists in reduced labels
+  std::vector<std::vector<uint32_t>> prefix;  // word taking the full set to each seed
+};
+
 class Solver {
  public:
   explicit Solver(int device);
@@ -29,9 +40,19 @@ class Solver {
   Solver& operator=(const Solver&) = delete;
 
   // Exact::run semantics on `b` (in/out).
-  void exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw_stats& st);
+  // With `red`, A is the reduced automaton and the search starts from the
+  // reduced BFS list (exact.cpp:130-146, 83-87).
+  void exact(const Automaton& A, const sw_exact_config& cfg, Bounds& b, sw_stats& st,
+             const ReduceState* red = nullptr);
+  // Reduce::run semantics: short dominance-pruned BFS from the full set; on
+  // success `red` describes the reduced automaton and the bounds are shifted.
+  void reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, sw_stats& st, ReduceState& red);
   // Beam::run semantics on `b` (in/out); also records a verified word.
   void beam(const Automaton& A, const sw_beam_config& cfg, Bounds& b, sw_stats& st);
+  // Eppstein::run semantics (greedy pair-merging upper bound and its word).
+  void eppstein(const Automaton& A, const sw_eppstein_config& cfg, Bounds& b, sw_stats& st);
+  // Brute::run semantics (power-set BFS, n <= 32): exact length and a word.
+  void brute(const Automaton& A, const sw_brute_config& cfg, Bounds& b, sw_stats& st);
 
   // Kernel-level helpers (reference bitset layout on the host).
   void apply_transition(const Automaton& A, uint32_t letter, bool inverse, const uint64_t* from, uint64_t* to,

@@ -788,12 +788,17 @@ void plan_from_json(const std::string& text, uint32_t n, uint32_t k, sw_plan* ou
       }
       if (presort != "none" && presort != "indeg") throw std::runtime_error("presort value not in [none, indeg]");
       alg.beam.presort_indeg = presort == "indeg";
-    } else if (name == "Brute") {
+    } else if (name == "Brute") {  // synchrolib/algorithm/brute/config.hpp:23-27
       alg.kind = SW_ALGO_BRUTE;
-    } else if (name == "Eppstein") {
+      alg.brute.max_n = value_of(cfg, "max_n", "20", n, k).as_u64();
+    } else if (name == "Eppstein") {  // synchrolib/algorithm/eppstein/config.hpp:23-31
       alg.kind = SW_ALGO_EPPSTEIN;
-    } else if (name == "Reduce") {
+      alg.eppstein.transition_tables = value_of(cfg, "transition_tables", "false", n, k, Key::Bool).as_bool();
+      alg.eppstein.find_word = value_of(cfg, "find_word", "false", n, k, Key::Bool).as_bool();
+    } else if (name == "Reduce") {  // synchrolib/algorithm/reduce/config.hpp:24-32
       alg.kind = SW_ALGO_REDUCE;
+      alg.reduce.min_n = value_of(cfg, "min_n", "80", n, k).as_u64();
+      alg.reduce.list_size_threshold = value_of(cfg, "list_size_threshold", "AUT_N * 16", n, k).as_u64();
     } else {
       throw std::runtime_error("Unknown algorithm: " + name);  // synchrolib.hpp:205
     }

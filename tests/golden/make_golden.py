@@ -80,7 +80,11 @@ def run_reference(plan: dict, autos, threads: int = 1, level: int = 3):
         m = re.match(r"(\d+): \[(\d+), (\d+)\] \((.*)\)", line)
         if m:
             ms = {a: int(t) for a, t in re.findall(r"\((\w+), (\d+)\)", m.group(4))}
-            results.append({"lower": int(m.group(2)), "upper": int(m.group(3)), "ms": ms})
+            res = {"lower": int(m.group(2)), "upper": int(m.group(3)), "ms": ms}
+            w = re.search(r"\{([\d ]*)\}\s*$", line)
+            if w:
+                res["word"] = [int(x) for x in w.group(1).split()]
+            results.append(res)
         elif "NON SYNCHRO" in line:
             results.append({"non_synchro": True})
     return results, traces
@@ -200,6 +204,89 @@ def fixture_batch(count=4096, seed=2026, sample=24):
                               "reference_checked_indices": checked, "oracle_seconds": round(oracle_s, 1)})
 
 
+EPPSTEIN = {"algorithms": [{"name": "Eppstein", "config": {"find_word": True}}]}
+
+
+def fixture_eppstein():
+    """Eppstein bounds and words from the reference (find_word on)."""
+    cases = []
+    inputs = [(n, k, seed, gen.random_dfa(n, k, seed)) for n, k, seed in
+              [(5, 2, 1), (12, 2, 2), (12, 3, 3), (30, 2, 4), (48, 2, 5), (64, 2, 6), (100, 2, 7), (100, 3, 8),
+               (200, 2, 9), (320, 2, 10), (384, 2, 11)]]
+    inputs += [(n, 2, None, gen.cerny(n)) for n in (4, 10, 20)]
+    inputs += [(6, 2, None, [1, 1, 2, 2, 0, 0, 4, 4, 5, 5, 3, 3])]  # two cycles: not synchronizing
+    for n, k, seed, d in inputs:
+        res, _ = run_reference(EPPSTEIN, [(n, k, d)])
+        r = res[0]
+        o, w = oracle.eppstein(d, n, k)
+        if r.get("non_synchro"):
+            assert o.non_synchro, (n, seed)
+        else:
+            assert (o.lower, o.upper) == (r["lower"], r["upper"]), (n, seed, r, o)
+            assert w == r.get("word"), (n, seed)
+        cases.append({"n": n, "k": k, "seed": seed, "delta": d if seed is None else None, "reference": r})
+    # a bound below the greedy length leaves the bounds unchanged (eppstein.hpp:104-106)
+    tight = dict(EPPSTEIN, upper_bound="5")
+    d = gen.random_dfa(48, 2, 5)
+    res, _ = run_reference(tight, [(48, 2, d)])
+    o, _ = oracle.eppstein(d, 48, 2, upper=5)
+    assert (o.lower, o.upper) == (res[0]["lower"], res[0]["upper"]) == (0, 5)
+    cases.append({"n": 48, "k": 2, "seed": 5, "delta": None, "upper_bound": "5", "reference": res[0]})
+    write("eppstein.json", {"plan": EPPSTEIN, "cases": cases})
+
+
+BRUTE = {"algorithms": [{"name": "Brute", "config": {"max_n": "24"}}]}
+
+
+def fixture_brute():
+    """Brute lengths from the reference for n <= 24."""
+    cases = []
+    for n, k, seed in [(6, 2, 1), (9, 3, 2), (12, 2, 3), (16, 2, 4), (18, 3, 5), (20, 2, 6), (22, 2, 7),
+                       (24, 2, 8), (24, 3, 9)]:
+        d = gen.random_dfa(n, k, seed)
+        res, _ = run_reference(BRUTE, [(n, k, d)])
+        want = oracle.brute(d, n, k)
+        r = res[0]
+        assert (want < 0 and r.get("non_synchro")) or (r["lower"], r["upper"]) == (want, want), (n, seed, r, want)
+        cases.append({"n": n, "k": k, "seed": seed, "reference": r})
+    write("brute.json", {"plan": BRUTE, "cases": cases})
+
+
+REDUCE_ONLY = {"algorithms": [{"name": "Reduce", "config": {}}]}
+
+
+def reference_reduce(plan, n, k, d):
+    """Reduce on the reference: (bounds line, reduced N, BFS steps) from its log."""
+    binary = build_ref.build(n, k, plan)
+    with tempfile.NamedTemporaryFile("w", suffix=".txt", delete=False) as f:
+        f.write(gen.to_text([(n, k, d)]))
+        path = f.name
+    r = subprocess.run([str(binary), "-f", path, "-L", "2"], capture_output=True, text=True, check=True)
+    m = re.search(r"Reduced to N = (\d+) in (\d+) bfs steps", r.stderr)
+    line = re.match(r"\d+: \[(\d+), (\d+)\]", r.stdout.strip())
+    out = {"lower": int(line.group(1)), "upper": int(line.group(2))} if line else {"raw": r.stdout.strip()}
+    if m:
+        out.update({"reduced_n": int(m.group(1)), "bfs_steps": int(m.group(2))})
+    elif "Skipping reduction" in r.stderr:
+        out["skipped"] = True
+    return out
+
+
+def fixture_reduce():
+    """Reduce outcomes (reduced N, BFS steps, shifted bounds) from the reference's log."""
+    cases = []
+    readme = json.loads((HERE / "readme.json").read_text())["automata"][3]
+    inputs = [(readme["n"], readme["k"], None, readme["delta"])]
+    inputs += [(n, k, seed, gen.random_dfa(n, k, seed)) for n, k, seed in
+               [(80, 2, 1), (100, 2, 2), (100, 3, 3), (128, 2, 4), (150, 2, 5), (200, 2, 6), (200, 3, 7),
+                (256, 2, 8)]]
+    for n, k, seed, d in inputs:
+        r = reference_reduce(REDUCE_ONLY, n, k, d)
+        cases.append({"n": n, "k": k, "seed": seed, "delta": d if seed is None else None, "reference": r})
+    assert cases[0]["reference"].get("reduced_n") == 90 and cases[0]["reference"]["bfs_steps"] == 8
+    write("reduce.json", {"plan": REDUCE_ONLY, "cases": cases})
+
+
 def fixture_big():
     for n in (320, 384):
         fixture_random(f"random_n{n}.json", n, 2, range(1, 9), {"beam_exact": BEAM_EXACT}, threads=8)
@@ -220,6 +307,9 @@ def main():
                                        with_trace=True),
         "beam": fixture_beam,
         "batch": fixture_batch,
+        "eppstein": fixture_eppstein,
+        "brute": fixture_brute,
+        "reduce": fixture_reduce,
     }
     if a.big:
         steps["big"] = fixture_big

@@ -1,0 +1,84 @@
+"""Reduce on the GPU: reduced state count, BFS steps and shifted bounds against
+the reference's own log (tests/golden/reduce.json), and Reduce followed by
+Exact against the plain exact length (the oracle) with the word checked on the
+original automaton."""
+import json
+from pathlib import Path
+
+import pytest
+
+import oracle
+from synchrowords_gb300.generate import random_dfa
+
+pytestmark = pytest.mark.gpu
+
+GOLD = Path(__file__).resolve().parent / "golden"
+
+# the settings of the reference's README run (configs/readme_config.json)
+README_PLAN = {
+    "upper_bound": "1ULL * AUT_N * AUT_N * AUT_N / 6", "threads": 1, "gpu": False,
+    "algorithms": [
+        {"name": "Brute", "config": {"max_n": "20"}},
+        {"name": "Eppstein", "config": {"transition_tables": False, "find_word": True}},
+        {"name": "Beam", "config": {"presort": "indeg", "beam_size": "10"}},
+        {"name": "Reduce", "config": {"min_n": "80", "list_size_threshold": "AUT_N * 16"}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "10000", "bfs_small_list_size": "AUT_N * 16",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "2 * 1024"}}]}
+
+
+def cases():
+    return json.loads((GOLD / "reduce.json").read_text())["cases"]
+
+
+def automaton(c):
+    return c["delta"] or random_dfa(c["n"], c["k"], c["seed"])
+
+
+@pytest.mark.parametrize("case", cases(), ids=lambda c: f"n{c['n']}k{c['k']}s{c['seed']}")
+def test_reduce_matches_reference_log(ctx, case):
+    n, k = case["n"], case["k"]
+    r = ctx.solve(automaton(case), n, k, json.dumps({"algorithms": [{"name": "Reduce", "config": {}}]}))
+    ref = case["reference"]
+    assert (r.lower, r.upper) == (ref["lower"], ref["upper"])
+    assert (r.stats["reduced_states"], r.stats["reduce_bfs_steps"]) == (ref["reduced_n"], ref["bfs_steps"])
+
+
+@pytest.mark.parametrize("case", cases(), ids=lambda c: f"n{c['n']}k{c['k']}s{c['seed']}")
+def test_reduce_then_exact_keeps_the_exact_length(ctx, case):
+    n, k = case["n"], case["k"]
+    d = automaton(case)
+    plan = {"algorithms": [{"name": "Reduce", "config": {}}, {"name": "Exact", "config": {}}]}
+    r = ctx.solve(d, n, k, json.dumps(plan))
+    ref = oracle.exact(d, n, k, oracle.ExactParams(threads=4))
+    assert (r.lower, r.upper) == (ref.lower, ref.upper)
+    assert r.word is not None and len(r.word) == r.upper
+    assert len(oracle.apply_word(d, n, k, r.word)) == 1
+
+
+def test_readme_run(ctx):
+    # data/readme_input.txt with configs/readme_config.json; expected lines of docs/install.md:101-104
+    g = json.loads((GOLD / "readme.json").read_text())
+    for a, exp in zip(g["automata"], g["expected"]):
+        n, k, d = a["n"], a["k"], a["delta"]
+        r = ctx.solve(d, n, k, json.dumps(README_PLAN))
+        if exp.get("non_synchro"):
+            assert r.non_synchro
+            continue
+        assert (r.lower, r.upper) == (exp["lower"], exp["upper"])
+        assert [name for name, _ in r.runs] == ["Brute", "Eppstein", "Beam", "Reduce", "Exact"]
+        if r.upper:
+            assert len(oracle.apply_word(d, n, k, r.word)) == 1
+
+
+def test_algorithms_after_reduce_leave_bounds_alone(ctx):
+    # Beam, Eppstein, Brute and Reduce refuse the reduced automaton (their
+    # "not compatible with inputs after reduction" branches); Exact then decides
+    c = cases()[0]
+    d = automaton(c)
+    plan = {"algorithms": [{"name": "Reduce", "config": {}}, {"name": "Beam", "config": {}},
+                           {"name": "Eppstein", "config": {}}, {"name": "Reduce", "config": {}}]}
+    r = ctx.solve(d, c["n"], c["k"], json.dumps(plan))
+    assert (r.lower, r.upper) == (c["reference"]["lower"], c["reference"]["upper"])
+    plan["algorithms"].append({"name": "Exact", "config": {}})
+    r = ctx.solve(d, c["n"], c["k"], json.dumps(plan))
+    assert r.lower == r.upper == 18

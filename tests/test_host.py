@@ -108,6 +108,13 @@ def test_plan_evaluation_matches_reference_defines(native_lib):
     assert beam["beam_exact_ratio"] == pytest.approx(0.01)
     ex = p["algorithms"][3]
     assert (ex["max_memory_mb"], ex["dfs_min_list_size"], ex["bfs_small_list_size"]) == (12288, 8192, 640)
+    assert p["algorithms"][0]["max_n"] == 15
+    assert (p["algorithms"][1]["transition_tables"], p["algorithms"][1]["find_word"]) == (0, 0)
+    others = sw.plan_from_json(json.dumps({"algorithms": [{"name": "Brute"}, {"name": "Eppstein"},
+                                                          {"name": "Reduce"}]}), 100, 3)
+    br, ep, rd = others["algorithms"]
+    assert br["max_n"] == 20 and (ep["transition_tables"], ep["find_word"]) == (0, 0)
+    assert (rd["min_n"], rd["list_size_threshold"]) == (80, 1600)
     d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "Exact", "config": {}}]}), 200, 2)
     assert d["upper_bound"] == 200 ** 3 // 6
     ex = d["algorithms"][0]

@@ -137,3 +137,28 @@ def test_oracle_matches_compiled_reference_random_n24():
     for (n, k, d), r in zip(autos, res):
         o = oracle.exact(d, n, k)
         assert (o.lower, o.upper) == (r["lower"], r["upper"])
+
+
+def test_oracle_eppstein_matches_reference_fixture():
+    g = load("eppstein.json")
+    for c in g["cases"]:
+        n, k = c["n"], c["k"]
+        d = c["delta"] or gen.random_dfa(n, k, c["seed"])
+        upper = int(c["upper_bound"]) if "upper_bound" in c else None
+        o, w = oracle.eppstein(d, n, k, upper=upper)
+        r = c["reference"]
+        if r.get("non_synchro"):
+            assert o.non_synchro
+            continue
+        assert (o.lower, o.upper) == (r["lower"], r["upper"])
+        assert w == r.get("word")
+
+
+def test_oracle_brute_matches_reference_fixture():
+    for c in load("brute.json")["cases"]:
+        d = gen.random_dfa(c["n"], c["k"], c["seed"])
+        want = oracle.brute(d, c["n"], c["k"])
+        r = c["reference"]
+        assert (want < 0) == bool(r.get("non_synchro"))
+        if want >= 0:
+            assert (r["lower"], r["upper"]) == (want, want)
