@@ -1,13 +1,14 @@
 // Shared definitions for the synchrowords GB300 library (host + device).
 //
 // Set layout on the device ("MSB-first rows"): a set of n states is a row of
-// W 64-bit words (W = 1, 2, 4 or 8: 64/128/256/512-bit classes); state q is
+// W 64-bit words (W = 1, 2 or 4 up to 256 states, else ceil(n/64) = 5..8,
+// so n = 320 / 384 use 40 / 48-byte rows, not 64); state q is
 // bit (63 - q % 64) of word q / 64.  With this layout the numeric order of
 // rows (word 0 most significant) is the reference's lexicographic order of
 // sets (state 0 most significant, synchrolib/data_structures/subset.hpp:71-77),
 // so one radix sort of raw words yields the order the prefix trie needs.
-// Unused tail bits are zero.  Rows are 8*W bytes and 16-byte aligned for W>=2
-// so warps move them as uint4.
+// Unused tail bits are zero.  Rows are 8*W bytes; row arrays start 16-byte
+// aligned, so 64-row tiles can be moved as uint4.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -40,7 +41,7 @@ constexpr int kMaxLetters = 16;
 
 inline int words_for(int n) {
   int w = (n + 63) / 64;
-  return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : 8;
+  return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : w;
 }
 
 // Device-side bit helpers for the MSB-first layout.

@@ -44,8 +44,6 @@ struct Side {
   u32 count = 0;
   DevBuf vis, vis_alt;
   u32 vis_count = 0;
-  DevBuf vis_gamma, vis_split;
-  DevBuf gamma, split;  // tree over `rows` (kept for F only)
   std::vector<std::unique_ptr<Layer>> layers;
   std::vector<u64> seed_states;  // backward side: the state of each seed row
   double unique_growth = 0;      // distinct children per parent at the last step
@@ -148,7 +146,7 @@ class Engine {
   // scratch
   DevBuf ch_rows, ch_vals, alt_rows, alt_vals, uq_rows, uq_vals, new_vals;
   DevBuf epp_scratch, epp_word, br_visited, br_arena;
-  DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, tmp_gamma, tmp_split, keys, keys_alt, sorted_rows;
+  DevBuf flags_a, flags_b, keep, pos, sort_tmp, scan_tmp, keys, keys_alt, sorted_rows;
 
   // Sort m rows in place by layer key (word 0, then a mix of the other words).
   void sort_by_layer_key(int W, u64* rows, u32 m, const KeyMap& map = KeyMap{}) {
@@ -220,40 +218,19 @@ class Engine {
     count_launch(launches);
   }
 
-  // Subset queries run on the tiled check (subset_check.cu); the radix-tree
-  // walk (kernels.cu) is kept as the alternative engine behind `use_tree`.
-  bool use_tree = false;
+  // Subset queries run on the tiled check (subset_check.cu).
   DevBuf tile_and;
 
-  void build_tree(int W, const u64* rows, u32 m, DevBuf& gamma, DevBuf& split) {
-    if (!use_tree || m < 2) return;
-    gamma.reserve(sizeof(u32) * m);
-    split.reserve(sizeof(u32) * m);
-    timed(3, (double)m * (8.0 * W * 2 + 8), [&] {
-      launch_trie_build(W, rows, m, gamma.as<u32>(), split.as<u32>(), stream);
-    });
-    count_launch();
-  }
-
-  void query(int W, int mode, const u64* S, u32 m, const DevBuf& gamma, const DevBuf& split, const u64* Q, u32 q,
-             int n, u32* flags, bool stop) {
+  void query(int W, int mode, const u64* S, u32 m, const u64* Q, u32 q, int n, u32* flags, bool stop) {
     if (!m || !q) return;
-    if (use_tree) {
-      timed(0, 0.0, [&] {
-        launch_trie_query(W, mode, S, m, m >= 2 ? gamma.as<u32>() : nullptr, m >= 2 ? split.as<u32>() : nullptr, Q,
-                          q, n, flags, d_misc, stop, stream, prof_on ? d_query_bytes : nullptr);
-      });
-      count_launch();
-    } else {
-      tile_and.reserve(subset_check_temp_bytes(W, m));
-      timed(3, (double)m * 8.0 * W, [&] { launch_tile_and(W, S, m, tile_and.as<u64>(), stream); });
-      // algorithmic bytes: the query rows plus every S tile staged on chip
-      timed(0, (double)q * 8.0 * W, [&] {
-        launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, stream,
-                            prof_on ? d_query_bytes : nullptr);
-      });
-      count_launch(2);
-    }
+    tile_and.reserve(subset_check_temp_bytes(W, m));
+    timed(3, (double)m * 8.0 * W, [&] { launch_tile_and(W, S, m, tile_and.as<u64>(), stream); });
+    // algorithmic bytes: the query rows plus every S tile staged on chip
+    timed(0, (double)q * 8.0 * W, [&] {
+      launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, stream,
+                          prof_on ? d_query_bytes : nullptr);
+    });
+    count_launch(2);
     if (st) {
       st->trie_queries += q;
       st->logical_pairs += (u64)m * q;
@@ -328,11 +305,10 @@ class Engine {
     count_launch(2);
     const double t_sort = vclock();
     if (X.vis_count)
-      query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split, uq_rows.as<u64>(), u, n,
+      query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, uq_rows.as<u64>(), u, n,
             flags_a.as<u32>(), false);
     const double t_vis = vclock();
-    build_tree(W, uq_rows.as<u64>(), u, tmp_gamma, tmp_split);
-    query(W, kQueryProperSubset, uq_rows.as<u64>(), u, tmp_gamma, tmp_split, uq_rows.as<u64>(), u, n,
+    query(W, kQueryProperSubset, uq_rows.as<u64>(), u, uq_rows.as<u64>(), u, n,
           flags_b.as<u32>(), false);
     const double t_self = vclock();
     if (verbose) {
@@ -377,7 +353,6 @@ class Engine {
     std::swap(X.vis.p, X.vis_alt.p);
     std::swap(X.vis.cap, X.vis_alt.cap);
     X.vis_count += f;
-    build_tree(W, X.vis.as<u64>(), X.vis_count, X.vis_gamma, X.vis_split);
     if (!X.keymap_chosen && X.count >= 2048) choose_keymap(X, W, n);
   }
 
@@ -453,7 +428,7 @@ class Engine {
   // query index and the F index.
   bool meet(int W, int n, const u64* Q, u32 q, u32* qi, u32* si) {
     SW_CUDA(cudaMemsetAsync(d_misc, 0, 4 * sizeof(u32), stream));
-    query(W, kQueryDisjoint, F.rows.as<u64>(), F.count, F.gamma, F.split, Q, q, n, nullptr, true);
+    query(W, kQueryDisjoint, F.rows.as<u64>(), F.count, Q, q, n, nullptr, true);
     if (st) st->meet_pairs += (u64)F.count * q;
     SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, stream));
     SW_CUDA(cudaStreamSynchronize(stream));
@@ -676,7 +651,6 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
                               E.stream));
       E.sort_by_layer_key(W, E.B.vis.as<u64>(), (u32)seeds.size());
       E.B.vis_count = (u32)seeds.size();
-      E.build_tree(W, E.B.vis.as<u64>(), E.B.vis_count, E.B.vis_gamma, E.B.vis_split);
     }
   }
   const size_t budget = (size_t)cfg.max_memory_mb * 1024 * 1024;
@@ -727,7 +701,6 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     if (!fwd && parents_before) b_growth = std::max(1.2, E.B.unique_growth);
     if (fwd) {
       st.bfs_steps++;
-      E.build_tree(W, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split);
     } else {
       st.ibfs_steps++;
     }
@@ -736,7 +709,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     SW_CUDA(cudaStreamSynchronize(E.stream));
     const auto t_meet_host0 = std::chrono::steady_clock::now();
     SW_CUDA(cudaMemsetAsync(E.d_misc, 0, 4 * sizeof(u32), E.stream));
-    E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.F.gamma, E.F.split, E.B.rows.as<u64>(), E.B.count,
+    E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.B.rows.as<u64>(), E.B.count,
             n, nullptr, true);
     st.meet_pairs += (u64)E.F.count * E.B.count;
     SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
@@ -1040,9 +1013,8 @@ void Solver::subsets_check(uint32_t n, const uint64_t* sets, uint64_t set_count,
   E.sort_rows(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), m);
   launch_unique_flags(W, E.uq_rows.as<u64>(), m, E.flags_a.as<u32>(), E.stream);
   u32 u = E.compact(W, E.uq_rows.as<u64>(), E.uq_vals.as<u32>(), E.flags_a.as<u32>(), m, E.keys.as<u64>(), nullptr);
-  E.build_tree(W, E.keys.as<u64>(), u, E.tmp_gamma, E.tmp_split);
   launch_fill_u32(E.flags_b.as<u32>(), 0, q, E.stream);
-  E.query(W, proper ? kQueryProperSubset : kQuerySubset, E.keys.as<u64>(), u, E.tmp_gamma, E.tmp_split,
+  E.query(W, proper ? kQueryProperSubset : kQuerySubset, E.keys.as<u64>(), u,
           E.ch_rows.as<u64>(), q, (int)n, E.flags_b.as<u32>(), false);
   std::vector<u32> flags(q);
   SW_CUDA(cudaMemcpyAsync(flags.data(), E.flags_b.p, sizeof(u32) * q, cudaMemcpyDeviceToHost, E.stream));

@@ -137,6 +137,9 @@ void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t
     SW_EXP(1)
     SW_EXP(2)
     SW_EXP(4)
+    SW_EXP(5)
+    SW_EXP(6)
+    SW_EXP(7)
     SW_EXP(8)
     default:
       throw std::runtime_error("expand: unsupported width");
@@ -640,11 +643,14 @@ __global__ void k_fill_u32(u32* p, u32 v, u32 m) {
     case 1: { constexpr int WW = 1; __VA_ARGS__; } break;   \
     case 2: { constexpr int WW = 2; __VA_ARGS__; } break;   \
     case 4: { constexpr int WW = 4; __VA_ARGS__; } break;   \
+    case 5: { constexpr int WW = 5; __VA_ARGS__; } break;   \
+    case 6: { constexpr int WW = 6; __VA_ARGS__; } break;   \
+    case 7: { constexpr int WW = 7; __VA_ARGS__; } break;   \
     case 8: { constexpr int WW = 8; __VA_ARGS__; } break;   \
     default: throw std::runtime_error("unsupported set width"); \
   }
 
-// Row widths of sort keys: set widths 1/2/4/8 and beam keys (1 + ceil(n/64)).
+// Row widths of sort keys: set widths 1..8 and beam keys (1 + set width).
 #define SW_DISPATCH_R(R, ...)                                 \
   switch (R) {                                                \
     case 1: { constexpr int RR = 1; __VA_ARGS__; } break;     \
@@ -693,216 +699,6 @@ void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t
 void launch_fill_u32(u32* p, u32 value, u32 m, cudaStream_t s) {
   if (!m) return;
   k_fill_u32<<<(m + 255) / 256, 256, 0, s>>>(p, value, m);
-  SW_LAUNCH_CHECK();
-}
-
-// ===========================================================================
-// Binary radix tree over sorted unique rows (Karras, "Maximizing parallelism
-// in the construction of BVHs, octrees, and k-d trees", HPG 2012).  Internal
-// node i covers [min(i,j), max(i,j)]; its keys share their first split[i]
-// bits; the left child [lo, gamma] has 0 at bit split[i], the right child
-// [gamma+1, hi] has 1.  This is the explicit form of the reference's implicit
-// trie recursion over bit depth (subsets_implicit_trie.hpp:224-265), with
-// constant-bit levels collapsed.
-// ===========================================================================
-template <int W>
-__device__ __forceinline__ int row_lcp(const u64* a, const u64* b) {
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    u64 x = a[w] ^ b[w];
-    if (x) return w * 64 + __clzll(x);
-  }
-  return W * 64;
-}
-
-template <int W>
-__global__ void k_trie_build(const u64* __restrict__ rows, u32 m, u32* __restrict__ gamma, u32* __restrict__ split) {
-  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= (long)m - 1) return;
-  const u64* ki = rows + (size_t)i * W;
-  auto L = [&](long j) -> int {
-    if (j < 0 || j >= (long)m) return -1;
-    return row_lcp<W>(ki, rows + (size_t)j * W);
-  };
-  const int d = (L(i + 1) - L(i - 1)) > 0 ? 1 : -1;
-  const int dmin = L(i - d);
-  long lmax = 2;
-  while (L(i + lmax * d) > dmin) lmax <<= 1;
-  long l = 0;
-  for (long t = lmax >> 1; t >= 1; t >>= 1)
-    if (L(i + (l + t) * d) > dmin) l += t;
-  const long j = i + l * d;
-  const int dnode = L(j);
-  long s = 0, t = l;
-  do {
-    t = (t + 1) >> 1;
-    if (L(i + (s + t) * d) > dnode) s += t;
-  } while (t > 1);
-  const long g = i + s * d + (d < 0 ? -1 : 0);
-  gamma[i] = (u32)g;
-  split[i] = (u32)dnode;
-}
-
-void launch_trie_build(int W, const u64* rows, u32 m, u32* gamma, u32* split, cudaStream_t s) {
-  if (m < 2) return;
-  SW_DISPATCH_W(W, (k_trie_build<WW><<<(m - 1 + 255) / 256, 256, 0, s>>>(rows, m, gamma, split)));
-  SW_LAUNCH_CHECK();
-}
-
-// ===========================================================================
-// Tree-walking subset query.  One thread per query row c; a depth-first walk
-// of the radix tree prunes (a) a subtree whose common key prefix has a state
-// that c lacks and (b) every right child (bit set) when c lacks the split
-// bit.  Ranges of at most kLeaf keys are tested directly.  The stack is
-// bounded; a range that does not fit is scanned linearly instead, so the walk
-// is exact for any tree depth.
-// ===========================================================================
-namespace {
-constexpr int kLeaf = 8;
-constexpr int kStack = 40;
-}  // namespace
-
-template <int W, int MODE>
-__global__ void __launch_bounds__(128) k_trie_query(const u64* __restrict__ S, u32 m, const u32* __restrict__ gamma,
-                                                    const u32* __restrict__ split, const u64* __restrict__ Q, u32 q,
-                                                    int n, u32* __restrict__ flags, u32* witness, int stop,
-                                                    u64* __restrict__ bytes_ctr) {
-  const u32 qi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (qi >= q) return;
-  u32 rows_read = 1, nodes_read = 0;  // algorithmic traffic: rows of W words, 8-byte node records
-  bool quit = stop && *(volatile u32*)witness;
-  u64 c[W];
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    c[w] = Q[(size_t)qi * W + w];
-    if (MODE == kQueryDisjoint) c[w] = ~c[w] & valid_mask(n, w);
-  }
-  auto test = [&](u32 idx) -> bool {
-    const u64* s = S + (size_t)idx * W;
-    ++rows_read;
-    bool eq = true;
-#pragma unroll
-    for (int w = 0; w < W; ++w) {
-      const u64 sv = s[w];
-      if (sv & ~c[w]) return false;
-      eq = eq && (sv == c[w]);
-    }
-    return MODE == kQueryProperSubset ? !eq : true;
-  };
-  bool hit = false;
-  u32 hit_idx = 0;
-  auto scan = [&](u32 lo, u32 hi) {
-    for (u32 x = lo; x <= hi; ++x)
-      if (test(x)) {
-        hit = true;
-        hit_idx = x;
-        return;
-      }
-  };
-  if (m == 0 || quit) {
-  } else if (m <= (u32)kLeaf) {
-    scan(0, m - 1);
-  } else {
-    u32 st_node[kStack], st_lo[kStack], st_hi[kStack];
-    int sp = 0;
-    st_node[0] = 0;
-    st_lo[0] = 0;
-    st_hi[0] = m - 1;
-    sp = 1;
-    int iter = 0;
-    while (sp > 0 && !hit) {
-      --sp;
-      const u32 x = st_node[sp], lo = st_lo[sp], hi = st_hi[sp];
-      if (hi - lo + 1 <= (u32)kLeaf) {
-        scan(lo, hi);
-        continue;
-      }
-      if (stop && ((++iter & 31) == 0) && *(volatile u32*)witness) {
-        quit = true;
-        break;
-      }
-      const u32 g = gamma[x], b = split[x];
-      nodes_read += 1;
-      rows_read += 1;
-      // (a) common prefix bits [0, b) of the range must lie inside c
-      bool ok = true;
-      const u64* s = S + (size_t)lo * W;
-#pragma unroll
-      for (int w = 0; w < W; ++w) {
-        const int base = w * 64;
-        if ((int)b > base) {
-          const u64 mask = ((int)b >= base + 64) ? ~0ULL : (~0ULL << (64 - ((int)b - base)));
-          if (s[w] & mask & ~c[w]) ok = false;
-        }
-      }
-      if (!ok) continue;
-      // (b) right child only if c has bit b
-      u64 cw = 0;
-#pragma unroll
-      for (int w = 0; w < W; ++w)
-        if (w == (int)(b >> 6)) cw = c[w];
-      const bool cb = (b < (u32)(W * 64)) && ((cw >> (63 - (b & 63))) & 1ULL);
-      if (cb) {
-        if (sp < kStack) {
-          st_node[sp] = g + 1;
-          st_lo[sp] = g + 1;
-          st_hi[sp] = hi;
-          ++sp;
-        } else {
-          scan(g + 1, hi);
-          if (hit) break;
-        }
-      }
-      if (sp < kStack) {
-        st_node[sp] = g;
-        st_lo[sp] = lo;
-        st_hi[sp] = g;
-        ++sp;
-      } else {
-        scan(lo, g);
-      }
-    }
-  }
-  if (bytes_ctr) {
-    const u32 mask = __activemask();
-    const u32 r = __reduce_add_sync(mask, rows_read), nd = __reduce_add_sync(mask, nodes_read);
-    if ((threadIdx.x & 31) == (u32)(__ffs(mask) - 1)) atomicAdd(bytes_ctr, (u64)r * (8 * W) + (u64)nd * 8);
-  }
-  if (!hit || quit) return;
-  if (stop) {
-    if (atomicCAS(witness, 0u, 1u) == 0u) {
-      witness[1] = qi;
-      witness[2] = hit_idx;
-    }
-  } else {
-    flags[qi] = 1u;
-  }
-}
-
-void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q, u32 q,
-                       int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s, u64* bytes_ctr) {
-  if (!q || !m) return;
-  const u32 blocks = (q + 127) / 128;
-#define SW_Q(WW)                                                                                                  \
-  case WW:                                                                                                        \
-    if (mode == kQuerySubset)                                                                                     \
-      k_trie_query<WW, kQuerySubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness, stop_at_first, bytes_ctr); \
-    else if (mode == kQueryProperSubset)                                                                          \
-      k_trie_query<WW, kQueryProperSubset><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,   \
-                                                                  stop_at_first, bytes_ctr);                      \
-    else                                                                                                          \
-      k_trie_query<WW, kQueryDisjoint><<<blocks, 128, 0, s>>>(S, m, gamma, split, Q, q, n, flags, witness,       \
-                                                              stop_at_first, bytes_ctr);                          \
-    break;
-  switch (W) {
-    SW_Q(1)
-    SW_Q(2)
-    SW_Q(4)
-    SW_Q(8)
-    default:
-      throw std::runtime_error("trie query: unsupported width");
-  }
-#undef SW_Q
   SW_LAUNCH_CHECK();
 }
 
@@ -1105,6 +901,37 @@ void launch_gather_rows(int W, const u64* src, const u32* idx, u32 m, u64* dst, 
 void launch_beam_keys(int W, const u64* rows, u32 m, int n, int R, u64* keys, cudaStream_t s) {
   if (!m) return;
   SW_DISPATCH_W(W, (k_beam_keys<WW><<<(m + 255) / 256, 256, 0, s>>>(rows, m, n, R, keys)));
+  SW_LAUNCH_CHECK();
+}
+
+__global__ void k_gather_u32(const u32* __restrict__ src, const u32* __restrict__ idx, u32 m, u32* __restrict__ dst) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < m) dst[i] = src[idx[i]];
+}
+
+void launch_gather_u32(const u32* src, const u32* idx, u32 m, u32* dst, cudaStream_t s) {
+  if (!m) return;
+  k_gather_u32<<<(m + 255) / 256, 256, 0, s>>>(src, idx, m, dst);
+  SW_LAUNCH_CHECK();
+}
+
+__global__ void k_score_keys(const float* __restrict__ score, const u32* __restrict__ counts, u32 m,
+                             u64* __restrict__ keys) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  u32 u;
+  if (score) {
+    u = __float_as_uint(score[i]);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);  // IEEE order -> unsigned order
+  } else {
+    u = counts[i];
+  }
+  keys[i] = ((u64)u << 32) | i;
+}
+
+void launch_score_keys(const float* score, const u32* counts, u32 m, u64* keys, cudaStream_t s) {
+  if (!m) return;
+  k_score_keys<<<(m + 255) / 256, 256, 0, s>>>(score, counts, m, keys);
   SW_LAUNCH_CHECK();
 }
 

@@ -8,9 +8,9 @@
 //                  cuda/preprocessed_transition_kernel.cu:19-88)
 //   radix sort +  sort_keep_unique (synchrolib/utils/vector.hpp:13-27)
 //   unique
-//   trie build +  SubsetsImplicitTrie::check_contains_subset / reduce
-//   trie query    (synchrolib/data_structures/subsets_implicit_trie.hpp:29-266,
-//                  cuda/subsets_implicit_trie_kernel.cu:13-92) and
+//   subset check  SubsetsImplicitTrie::check_contains_subset / reduce
+//   (subset_      (synchrolib/data_structures/subsets_implicit_trie.hpp:29-266,
+//   check.cu)      cuda/subsets_implicit_trie_kernel.cu:13-92) and
 //                 SubsetsTrie::contains_subset_of (subsets_trie.hpp:78-90)
 #pragma once
 #include "common.cuh"
@@ -51,30 +51,19 @@ void launch_unique_flags(int W, const u64* rows, u32 m, u32* flags, cudaStream_t
 void launch_compact(int W, const u64* rows, const u32* vals, const u32* flags, const u32* pos, u32 m, u64* out_rows,
                     u32* out_vals, cudaStream_t s);
 
-// Binary radix tree (Karras 2012) over m >= 2 sorted unique rows: node i in
-// [0, m-2] gets its split position gamma[i] and the first differing bit
-// split[i] of its key range.
-void launch_trie_build(int W, const u64* rows, u32 m, u32* gamma, u32* split, cudaStream_t s);
-
 enum QueryMode : int {
   kQuerySubset = 0,        // hit(c) = exists s in S, s ⊆ c
   kQueryProperSubset = 1,  // hit(c) = exists s in S, s ⊊ c
   kQueryDisjoint = 2,      // hit(c) = exists s in S, s ∩ c = ∅  (s ⊆ ~c)
 };
 
-// Trie query: for each query row c, flags[c] |= hit(c) (or, with
-// `stop_at_first`, record one witness pair and let all threads exit early).
-// witness[0] = found flag, witness[1] = query index, witness[2] = set index.
-// `bytes_ctr` (optional) accumulates the algorithmic bytes the walk reads:
-// 8*W per row compared (query, prefix and leaf rows) + 8 per tree node.
-void launch_trie_query(int W, int mode, const u64* S, u32 m, const u32* gamma, const u32* split, const u64* Q,
-                       u32 q, int n, u32* flags, u32* witness, bool stop_at_first, cudaStream_t s,
-                       u64* bytes_ctr = nullptr);
-
-// Tiled subset check (subset_check.cu), same semantics as launch_trie_query:
-// S sorted, cut into 64-row tiles; tile_and[t] (W words) = AND of the tile's
-// rows, from launch_tile_and.  `flags` must start zeroed (non-stop mode).
-// `bytes_ctr` (optional) accumulates the bytes of S tiles staged on chip.
+// Tiled subset check (subset_check.cu): for each query row c, flags[c] |=
+// hit(c) (or, with `stop`, record one witness pair and let all warps exit
+// early: witness[0] = found flag, witness[1] = query index, witness[2] = set
+// index).  S is cut into 64-row tiles; tile_and[t] (W words) = AND of the
+// tile's rows, from launch_tile_and.  `flags` must start zeroed (non-stop
+// mode).  `bytes_ctr` (optional) accumulates the bytes of S tiles staged on
+// chip.
 size_t subset_check_temp_bytes(int W, u32 m);
 void launch_tile_and(int W, const u64* S, u32 m, u64* tile_and, cudaStream_t s);
 void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* tile_and, const u64* Q, u32 q, int n,
@@ -117,6 +106,13 @@ void launch_gather_rows(int W, const u64* src, const u32* idx, u32 m, u64* dst, 
 
 // Beam sort keys: keys[i] = [n - |row i|, bit-reversed words of row i] (R words).
 void launch_beam_keys(int W, const u64* rows, u32 m, int n, int R, u64* keys, cudaStream_t s);
+
+// dst[i] = src[idx[i]] (u32 payloads).
+void launch_gather_u32(const u32* src, const u32* idx, u32 m, u32* dst, cudaStream_t s);
+
+// Ascending sort keys of beam candidates: keys[i] = (order-preserving bits of
+// score[i]) << 32 | i, from float scores or (when score is null) u32 counts.
+void launch_score_keys(const float* score, const u32* counts, u32 m, u64* keys, cudaStream_t s);
 
 // Fill u32 array with a value.
 void launch_fill_u32(u32* p, u32 value, u32 m, cudaStream_t s);

@@ -88,6 +88,16 @@ def test_random_n200_exact(ctx, seed):
     check_word(d, n, k, r)
 
 
+@pytest.mark.parametrize("n,seed", [(270, 1), (300, 4), (330, 12), (330, 13), (400, 34)])
+def test_random_wide_rows_exact(ctx, n, seed):
+    # five-, six- and seven-word rows (n = 257..448); seeds the oracle solves in seconds
+    d = random_dfa(n, 2, seed)
+    r = ctx.solve(d, n, 2, EXACT)
+    ref = oracle.exact(d, n, 2, oracle.ExactParams(threads=8))
+    assert (r.lower, r.upper) == (ref.lower, ref.upper)
+    check_word(d, n, 2, r)
+
+
 @pytest.mark.parametrize("seed", [5, 6])
 def test_random_n200_beam_exact(ctx, seed):
     n, k = 200, 2

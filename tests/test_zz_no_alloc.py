@@ -19,9 +19,9 @@ pytestmark = pytest.mark.gpu
 
 
 def device_rows(sets, n):
-    """Rows in the device layout: W in {1, 2, 4, 8} words, state q at bit 63 - q % 64 of word q / 64."""
+    """Rows in the device layout: W = 1, 2, 4, then ceil(n/64) words, state q at bit 63 - q % 64 of word q / 64."""
     w = (n + 63) // 64
-    W = 1 if w <= 1 else 2 if w <= 2 else 4 if w <= 4 else 8
+    W = 1 if w <= 1 else 2 if w <= 2 else 4 if w <= 4 else w
     out = np.zeros((len(sets), W), dtype=np.uint64)
     for i, s in enumerate(sets):
         for q in s:
@@ -55,6 +55,11 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx, native_lib):
     S2 = random_sets(rng, n2, 700, 0.15)
     C2 = random_sets(rng, n2, 900, 0.6) + S2[:30] + [frozenset(range(n2))]
     cases.append((n2, S2, C2, True))
+    # third: 320 states (five-word rows, an odd word count per tile)
+    n3 = 320
+    S3 = random_sets(rng, n3, 1001, 0.08)
+    C3 = random_sets(rng, n3, 800, 0.8) + S3[:20]
+    cases.append((n3, S3, C3, False))
     for n, S, C, proper in cases:
         want = ctx.subsets_check(n, to_rows(S, n), to_rows(C, n), proper=proper).tolist()
         got = run_noalloc(native_lib, n, S, C, proper)
