@@ -46,6 +46,14 @@ PLAN_BEAM_EXACT = json.dumps({
         {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
                                      "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
 
+# the same Exact entry, its upper bound from the learned forward beam instead
+PLAN_LEARNED_EXACT = json.dumps({
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1",
+    "algorithms": [
+        {"name": "LearnedBeam", "config": {"beam_size": "4096", "order": "model"}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
+
 WORKLOADS = {
     # name: (n, k, count, plan, description); n = 0 marks the uneven batch
     "n200": (200, 2, 16, PLAN_EXACT, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
@@ -54,7 +62,14 @@ WORKLOADS = {
                   "plain exact, 4096 random DFAs, n ~ U[32,160], k ~ U{2,3} (64/128/256-bit sets)"),
     "n320": (320, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=320"),
     "n384": (384, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=384"),
+    "n384_learned": (384, 2, 8, PLAN_LEARNED_EXACT,
+                     "LearnedBeam(4096, distance model)+Exact, 8 random binary DFAs, n=384"),
 }
+
+
+def plan_name(plan: str) -> str:
+    return {PLAN_EXACT: "Exact (defaults)", PLAN_BEAM_EXACT: "Beam(dynamic)+Exact",
+            PLAN_LEARNED_EXACT: "LearnedBeam+Exact"}[plan]
 
 
 def workload_dfas(name: str, rank: int):
@@ -161,7 +176,7 @@ def cpu_baseline(dfas, sample: int, threads: int, plan: str = PLAN_EXACT):
     t0 = time.perf_counter()
     lengths = []
     for n, k, d in dfas[:sample]:
-        if plan == PLAN_BEAM_EXACT:
+        if plan in (PLAN_BEAM_EXACT, PLAN_LEARNED_EXACT):  # the reference has no learned beam: its own plan
             lg = math.log2(n)
             b = oracle.beam(d, n, k, oracle.BeamParams(dynamic=True, presort_indeg=True, min_beam_size=int(n * lg),
                                                        max_beam_size=int(n * n * lg)), upper=(n - 1) ** 2 + 1)
@@ -196,8 +211,7 @@ def run_reference(args, world, rank):
         "ms_per_step": round(value * per_step, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": desc, "n": n, "k": k, "dfas_per_step": per_step,
-                   "plan": "Exact (defaults)" if plan == PLAN_EXACT else "Beam(dynamic)+Exact",
-                   "l2": "host-only run"},
+                   "plan": plan_name(plan), "l2": "host-only run"},
         "cpu_baseline": {"value": round(value, 4), "unit": "ms", "cores": threads, "kind": "port",
                          "sample": f"{per_step} DFAs per step out of {count}, rotating"},
         "e2e": {"value": round(value, 4), "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -305,7 +319,7 @@ def run_ours(args, world, rank, local):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(dev_total / args.steps, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": "Exact (defaults)" if plan == PLAN_EXACT else "Beam(dynamic)+Exact",
+        "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": plan_name(plan),
                    "streams": args.streams,
                    "l2": "flushed (256 MB write) before every timed step", "per_gpu_ms_per_dfa": round(value, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

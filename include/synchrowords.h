@@ -50,7 +50,8 @@ typedef enum {
   SW_ALGO_BEAM = 2,     /* synchrolib/algorithm/beam/ */
   SW_ALGO_BRUTE = 3,    /* synchrolib/algorithm/brute/ */
   SW_ALGO_EPPSTEIN = 4, /* synchrolib/algorithm/eppstein/ */
-  SW_ALGO_REDUCE = 5    /* synchrolib/algorithm/reduce/ */
+  SW_ALGO_REDUCE = 5,   /* synchrolib/algorithm/reduce/ */
+  SW_ALGO_LEARNED_BEAM = 6 /* no reference counterpart: forward beam scored by the learned model */
 } sw_algo_kind;
 
 /* Evaluated Exact defines (synchrolib/algorithm/exact/config.hpp:24-46). */
@@ -92,6 +93,21 @@ typedef struct {
   uint64_t list_size_threshold; /* "list_size_threshold" (default AUT_N * 16) */
 } sw_reduce_config;
 
+/* "LearnedBeam" (no reference counterpart): a forward beam from the full set
+ * that keeps the `beam_size` best children of each layer; the first
+ * singleton gives an upper bound and its word.  "order" ranks children by
+ * "model" (smallest predicted merge length, the context's distance model),
+ * "size" (fewest states; no model needed) or "size_model" (fewest states,
+ * ties by predicted merge length). */
+#define SW_ORDER_MODEL 0
+#define SW_ORDER_SIZE 1
+#define SW_ORDER_SIZE_MODEL 2
+typedef struct {
+  uint64_t beam_size; /* "beam_size" (default 4096) */
+  int64_t max_iter;   /* "max_iter" (default -1: up to the upper bound) */
+  int32_t order;      /* "order" (default "model"): SW_ORDER_* */
+} sw_learned_beam_config;
+
 typedef struct {
   int32_t kind; /* sw_algo_kind */
   char name[SW_NAME_LEN];
@@ -100,6 +116,7 @@ typedef struct {
   sw_brute_config brute;
   sw_eppstein_config eppstein;
   sw_reduce_config reduce;
+  sw_learned_beam_config learned_beam;
 } sw_algorithm;
 
 /* Global plan keys (app/jit.hpp:112-141, docs/config.md:15-27). */
@@ -235,6 +252,50 @@ int sw_subsets_check(sw_context* ctx, uint32_t n, const uint64_t* sets, uint64_t
  * sets in place; *out_count receives the number kept.  Replaces
  * sort_keep_unique (synchrolib/utils/vector.hpp:13-27). */
 int sw_sort_unique(sw_context* ctx, uint32_t n, uint64_t* sets, uint64_t count, uint64_t* out_count);
+
+/* ---- learned distance model (no reference counterpart) -------------------
+ * A set S is scored by y = w3 · relu(W2 relu(W1 x + b1) + b2) + b3 with
+ * x = sum over q in S of relu(feat(q) · Phi + c): per-state BF16 embeddings
+ * from fixed per-state features (so one model fits automata of any size),
+ * dense layers 64 -> 128 -> 128 on the tensor cores with FP32 accumulation.
+ * Parameters are SW_MLP_PARAMS floats: Phi[16][64], c[64], W1[64][128],
+ * b1[128], W2[128][128], b2[128], w3[128], b3.  Sets passed to these calls
+ * use 8 words per set in the reference bit layout (state q = bit q % 64 of
+ * word q / 64). */
+#define SW_MLP_PARAMS 26049
+#define SW_STATE_FEATURES 16
+
+/* The model a context's LearnedBeam uses (copied; replaces the previous one). */
+int sw_context_set_model(sw_context* ctx, const float* params, uint32_t count);
+int sw_context_get_model(sw_context* ctx, float* params, uint32_t count);
+
+/* Per-state feature rows of an automaton: out[n * SW_STATE_FEATURES]. */
+int sw_state_features(const uint32_t* delta, uint32_t n, uint32_t k, float* out);
+
+/* Training pairs: sets of the dominance-pruned forward BFS layers of the
+ * automaton (at most `per_layer` per layer, evenly spread), each labelled
+ * with its exact shortest merge length, found by subset queries against the
+ * inverse BFS layers from the singletons (labels above the inverse depth
+ * reached are censored to that depth + 1); depths[i] = the forward layer of
+ * set i (may be NULL).  *length = the reset length. */
+int sw_distance_pairs(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, uint32_t per_layer,
+                      uint64_t max_inverse_sets, uint64_t* sets, float* labels, uint32_t* depths, uint64_t capacity,
+                      uint64_t* count, uint32_t* length);
+
+/* Model output for `count` sets of one automaton (loads `params` into ctx). */
+int sw_mlp_forward(sw_context* ctx, const float* params, const uint32_t* delta, uint32_t n, uint32_t k,
+                   const uint64_t* sets, uint64_t count, float* out);
+
+/* Gradient of the mean squared error over the batch (loads `params`). */
+int sw_mlp_gradient(sw_context* ctx, const float* params, const uint32_t* delta, uint32_t n, uint32_t k,
+                    const uint64_t* sets, const float* labels, uint64_t count, float* grad, float* loss);
+
+/* Adam training over labelled sets of many automata; pairs of automaton i
+ * are [offsets[i], offsets[i+1]).  `params` in: start, out: trained (also
+ * loaded into ctx).  *loss = mean batch loss of the last epoch. */
+int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32_t* deltas, const uint32_t* ns,
+                 const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets, const float* labels,
+                 uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* loss);
 
 /* ---- allocation-free variant --------------------------------------------
  * No counterpart in the reference (its GPU helpers cudaMalloc and cudaFree

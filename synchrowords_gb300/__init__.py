@@ -63,9 +63,14 @@ class _ReduceCfg(ctypes.Structure):
     _fields_ = [("min_n", ctypes.c_uint64), ("list_size_threshold", ctypes.c_uint64)]
 
 
+class _LearnedBeamCfg(ctypes.Structure):
+    _fields_ = [("beam_size", ctypes.c_uint64), ("max_iter", ctypes.c_int64), ("order", ctypes.c_int32)]
+
+
 class _Algo(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int32), ("name", ctypes.c_char * NAME_LEN), ("exact", _ExactCfg),
-                ("beam", _BeamCfg), ("brute", _BruteCfg), ("eppstein", _EppsteinCfg), ("reduce", _ReduceCfg)]
+                ("beam", _BeamCfg), ("brute", _BruteCfg), ("eppstein", _EppsteinCfg), ("reduce", _ReduceCfg),
+                ("learned_beam", _LearnedBeamCfg)]
 
 
 class _Plan(ctypes.Structure):
@@ -136,6 +141,18 @@ def load_library():
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                                      ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_void_p]
+    _F32P = ctypes.POINTER(ctypes.c_float)
+    lib.sw_context_set_model.argtypes = [ctypes.c_void_p, _F32P, ctypes.c_uint32]
+    lib.sw_context_get_model.argtypes = [ctypes.c_void_p, _F32P, ctypes.c_uint32]
+    lib.sw_state_features.argtypes = [_U32P, ctypes.c_uint32, ctypes.c_uint32, _F32P]
+    lib.sw_distance_pairs.argtypes = [ctypes.c_void_p, _U32P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.c_uint64, _U64P, _F32P, _U32P, ctypes.c_uint64, _U64P, _U32P]
+    lib.sw_mlp_forward.argtypes = [ctypes.c_void_p, _F32P, _U32P, ctypes.c_uint32, ctypes.c_uint32, _U64P,
+                                   ctypes.c_uint64, _F32P]
+    lib.sw_mlp_gradient.argtypes = [ctypes.c_void_p, _F32P, _U32P, ctypes.c_uint32, ctypes.c_uint32, _U64P, _F32P,
+                                    ctypes.c_uint64, _F32P, _F32P]
+    lib.sw_mlp_train.argtypes = [ctypes.c_void_p, _F32P, ctypes.c_uint32, _U32P, _U32P, _U32P, _U64P, _U64P, _F32P,
+                                 ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64, _F32P]
     lib.sw_profile_begin.argtypes = [ctypes.c_void_p]
     lib.sw_profile_end.argtypes = [ctypes.c_void_p, ctypes.POINTER(_KernelProfile)]
     lib.sw_context_stream.argtypes = [ctypes.c_void_p]
@@ -179,6 +196,8 @@ def plan_from_json(text: str, n: int, k: int) -> dict:
             d.update({f: getattr(a.eppstein, f) for f, _ in _EppsteinCfg._fields_})
         elif a.kind == 5:
             d.update({f: getattr(a.reduce, f) for f, _ in _ReduceCfg._fields_})
+        elif a.kind == 6:
+            d.update({f: getattr(a.learned_beam, f) for f, _ in _LearnedBeamCfg._fields_})
         algos.append(d)
     return {"upper_bound": p.upper_bound, "threads": p.threads, "gpu": p.gpu,
             "gpu_max_memory_mb": p.gpu_max_memory_mb, "algorithms": algos}
@@ -195,13 +214,104 @@ class Result:
     stats: dict = field(default_factory=dict)
 
 
-class Context:
-    """One CUDA device with persistent buffers (not thread-safe)."""
+MLP_PARAMS = 26049
+STATE_FEATURES = 16
+DEFAULT_MODEL = Path(__file__).resolve().parent / "models" / "distance_mlp.f32"
+_F32 = ctypes.POINTER(ctypes.c_float)
 
-    def __init__(self, device: int = 0):
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def load_model(path=DEFAULT_MODEL) -> np.ndarray:
+    """Parameters of the learned distance model (MLP_PARAMS little-endian float32)."""
+    p = np.fromfile(str(path), dtype="<f4")
+    if p.size != MLP_PARAMS:
+        raise ValueError(f"{path}: expected {MLP_PARAMS} floats, found {p.size}")
+    return p.astype(np.float32)
+
+
+def state_features(delta: Sequence[int], n: int, k: int) -> np.ndarray:
+    out = np.zeros((n, STATE_FEATURES), dtype=np.float32)
+    _check(load_library().sw_state_features(_u32(delta).ctypes.data_as(_U32P), n, k, out.ctypes.data_as(_F32)))
+    return out
+
+
+class Context:
+    """One CUDA device with persistent buffers (not thread-safe).
+
+    The packaged distance model (models/distance_mlp.f32), when present, is
+    loaded so that plans with a LearnedBeam entry run as they are."""
+
+    def __init__(self, device: int = 0, model=DEFAULT_MODEL):
         self._lib = load_library()
         self._h = ctypes.c_void_p()
         _check(self._lib.sw_context_create(device, ctypes.byref(self._h)))
+        if model is not None and Path(model).exists():
+            self.set_model(load_model(model))
+
+    def set_model(self, params) -> None:
+        p = _f32(params)
+        _check(self._lib.sw_context_set_model(self._h, p.ctypes.data_as(_F32), p.size))
+
+    def get_model(self) -> np.ndarray:
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        _check(self._lib.sw_context_get_model(self._h, p.ctypes.data_as(_F32), MLP_PARAMS))
+        return p
+
+    def distance_pairs(self, delta, n: int, k: int, per_layer: int = 256, max_inverse_sets: int = 4_000_000,
+                       capacity: int = 1 << 20):
+        """(sets [count, 8] uint64 in the reference layout, labels float32,
+        forward depths uint32, reset length)."""
+        sets = np.zeros((capacity, 8), dtype=np.uint64)
+        labels = np.zeros(capacity, dtype=np.float32)
+        depths = np.zeros(capacity, dtype=np.uint32)
+        cnt, length = ctypes.c_uint64(), ctypes.c_uint32()
+        _check(self._lib.sw_distance_pairs(self._h, _u32(delta).ctypes.data_as(_U32P), n, k, per_layer,
+                                           max_inverse_sets, sets.ctypes.data_as(_U64P), labels.ctypes.data_as(_F32),
+                                           depths.ctypes.data_as(_U32P), capacity, ctypes.byref(cnt),
+                                           ctypes.byref(length)))
+        c = cnt.value
+        return sets[:c].copy(), labels[:c].copy(), depths[:c].copy(), length.value
+
+    def mlp_forward(self, params, delta, n: int, k: int, sets: np.ndarray) -> np.ndarray:
+        s = np.ascontiguousarray(sets, dtype=np.uint64).reshape(-1, 8)
+        out = np.zeros(len(s), dtype=np.float32)
+        p = _f32(params)
+        _check(self._lib.sw_mlp_forward(self._h, p.ctypes.data_as(_F32), _u32(delta).ctypes.data_as(_U32P), n, k,
+                                        s.ctypes.data_as(_U64P), len(s), out.ctypes.data_as(_F32)))
+        return out
+
+    def mlp_gradient(self, params, delta, n: int, k: int, sets: np.ndarray, labels) -> Tuple[np.ndarray, float]:
+        s = np.ascontiguousarray(sets, dtype=np.uint64).reshape(-1, 8)
+        t = _f32(labels)
+        g = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_float()
+        p = _f32(params)
+        _check(self._lib.sw_mlp_gradient(self._h, p.ctypes.data_as(_F32), _u32(delta).ctypes.data_as(_U32P), n, k,
+                                         s.ctypes.data_as(_U64P), t.ctypes.data_as(_F32), len(s),
+                                         g.ctypes.data_as(_F32), ctypes.byref(loss)))
+        return g, loss.value
+
+    def mlp_train(self, params, automata, sets_per_automaton, labels_per_automaton, epochs: int = 1,
+                  batch: int = 512, lr: float = 1e-3, seed: int = 1) -> Tuple[np.ndarray, float]:
+        """Adam training; returns (trained parameters, mean batch loss of the last epoch)."""
+        p = _f32(params).copy()
+        deltas = np.concatenate([_u32(d) for _, _, d in automata])
+        ns = _u32([n for n, _, _ in automata])
+        ks = _u32([k for _, k, _ in automata])
+        offs = np.zeros(len(automata) + 1, dtype=np.uint64)
+        offs[1:] = np.cumsum([len(l) for l in labels_per_automaton])
+        sets = np.ascontiguousarray(np.concatenate([np.asarray(s, dtype=np.uint64).reshape(-1, 8)
+                                                    for s in sets_per_automaton]), dtype=np.uint64)
+        labels = _f32(np.concatenate(labels_per_automaton))
+        loss = ctypes.c_float()
+        _check(self._lib.sw_mlp_train(self._h, p.ctypes.data_as(_F32), len(automata), deltas.ctypes.data_as(_U32P),
+                                      ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P), offs.ctypes.data_as(_U64P),
+                                      sets.ctypes.data_as(_U64P), labels.ctypes.data_as(_F32), epochs, batch, lr,
+                                      seed, ctypes.byref(loss)))
+        return p, loss.value
 
     def close(self) -> None:
         if self._h:

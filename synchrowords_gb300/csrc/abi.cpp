@@ -137,7 +137,7 @@ int run_plan(sw::Solver& solver, const uint32_t* delta, uint32_t n, uint32_t k, 
     const sw_algorithm& alg = plan->algorithms[i];
     auto t0 = std::chrono::steady_clock::now();
     if (red.active && alg.kind != SW_ALGO_EXACT) {
-      if (alg.kind < SW_ALGO_EXACT || alg.kind > SW_ALGO_REDUCE) {
+      if (alg.kind < SW_ALGO_EXACT || alg.kind > SW_ALGO_LEARNED_BEAM) {
         err = std::string("algorithm ") + alg.name + " is outside this library's scope";
         return SW_ERR_UNSUPPORTED;
       }
@@ -160,6 +160,9 @@ int run_plan(sw::Solver& solver, const uint32_t* delta, uint32_t n, uint32_t k, 
           break;
         case SW_ALGO_REDUCE:
           solver.reduce(A, alg.reduce, b, r->stats, red);
+          break;
+        case SW_ALGO_LEARNED_BEAM:
+          solver.learned_beam(A, alg.learned_beam, b, r->stats);
           break;
         default:
           err = std::string("algorithm ") + alg.name + " is outside this library's scope";
@@ -302,6 +305,94 @@ int sw_sort_unique(sw_context* ctx, uint32_t n, uint64_t* sets, uint64_t count, 
   if (!ctx || !out_count || (count && !sets)) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
   return guarded([&] {
     *out_count = ctx->solver->sort_unique(n, sets, count);
+    return SW_OK;
+  });
+}
+
+// ---- learned distance model --------------------------------------------------
+int sw_context_set_model(sw_context* ctx, const float* params, uint32_t count) {
+  if (!ctx || !params) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (count != SW_MLP_PARAMS) return fail(SW_ERR_INVALID_ARGUMENT, "model must have SW_MLP_PARAMS floats");
+  return guarded([&] {
+    ctx->solver->set_model(params);
+    return SW_OK;
+  });
+}
+
+int sw_context_get_model(sw_context* ctx, float* params, uint32_t count) {
+  if (!ctx || !params) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (count != SW_MLP_PARAMS) return fail(SW_ERR_INVALID_ARGUMENT, "model must have SW_MLP_PARAMS floats");
+  return guarded([&] {
+    ctx->solver->get_model(params);
+    return SW_OK;
+  });
+}
+
+int sw_state_features(const uint32_t* delta, uint32_t n, uint32_t k, float* out) {
+  if (!delta || !out) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    const std::vector<float> f = sw::state_features(sw::make_automaton(delta, n, k));
+    std::memcpy(out, f.data(), sizeof(float) * f.size());
+    return SW_OK;
+  });
+}
+
+int sw_distance_pairs(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, uint32_t per_layer,
+                      uint64_t max_inverse_sets, uint64_t* sets, float* labels, uint32_t* depths, uint64_t capacity,
+                      uint64_t* count, uint32_t* length) {
+  if (!ctx || !delta || !count || !length || (capacity && (!sets || !labels)))
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    std::vector<uint64_t> s;
+    std::vector<float> l;
+    std::vector<uint32_t> dep;
+    *length = ctx->solver->distance_pairs(sw::make_automaton(delta, n, k), per_layer, max_inverse_sets, s, l, dep);
+    *count = l.size();
+    if (l.size() > capacity) return fail(SW_ERR_CAPACITY, "pair buffer too small");
+    std::memcpy(sets, s.data(), sizeof(uint64_t) * s.size());
+    std::memcpy(labels, l.data(), sizeof(float) * l.size());
+    if (depths) std::memcpy(depths, dep.data(), sizeof(uint32_t) * dep.size());
+    return SW_OK;
+  });
+}
+
+int sw_mlp_forward(sw_context* ctx, const float* params, const uint32_t* delta, uint32_t n, uint32_t k,
+                   const uint64_t* sets, uint64_t count, float* out) {
+  if (!ctx || !params || !delta || (count && (!sets || !out))) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    ctx->solver->set_model(params);
+    ctx->solver->mlp_forward(sw::make_automaton(delta, n, k), sets, count, out);
+    return SW_OK;
+  });
+}
+
+int sw_mlp_gradient(sw_context* ctx, const float* params, const uint32_t* delta, uint32_t n, uint32_t k,
+                    const uint64_t* sets, const float* labels, uint64_t count, float* grad, float* loss) {
+  if (!ctx || !params || !delta || !sets || !labels || !grad || !loss || !count)
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument or empty batch");
+  return guarded([&] {
+    ctx->solver->set_model(params);
+    *loss = ctx->solver->mlp_gradient(sw::make_automaton(delta, n, k), sets, labels, count, grad);
+    return SW_OK;
+  });
+}
+
+int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32_t* deltas, const uint32_t* ns,
+                 const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets, const float* labels,
+                 uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* loss) {
+  if (!ctx || !params || !deltas || !ns || !ks || !offsets || !sets || !labels || !loss)
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  return guarded([&] {
+    std::vector<sw::Automaton> autos;
+    size_t off = 0;
+    for (uint32_t i = 0; i < automata; ++i) {
+      autos.push_back(sw::make_automaton(deltas + off, ns[i], ks[i]));
+      off += (size_t)ns[i] * ks[i];
+      if (offsets[i + 1] < offsets[i]) throw std::invalid_argument("pair offsets must not decrease");
+    }
+    ctx->solver->set_model(params);
+    *loss = ctx->solver->mlp_train(autos, offsets, sets, labels, epochs, batch, lr, seed);
+    ctx->solver->get_model(params);
     return SW_OK;
   });
 }

@@ -33,6 +33,15 @@ Automaton permute(const Automaton& A, const std::vector<uint32_t>& order);
 // word; the search would otherwise run to its upper bound.
 bool is_synchronizing(const Automaton& A);
 
+// Per-state feature vectors of the learned distance model (n rows of
+// `kStateFeatures` floats): structural quantities that mean the same thing in
+// automata of any size (in-degrees, stationary mass of a random-letter walk,
+// sink membership, collisions, shortest merge lengths with the other states),
+// standardised over the states, plus a
+// constant one and 64 / n, so one trained model scores sets of any automaton.
+constexpr int kStateFeatures = 16;
+std::vector<float> state_features(const Automaton& A);
+
 // Per-letter device tables (u16): delta[a*n + q]; inverse CSR inv_beg[a*(n+1) + t],
 // inv_src[a*n + e].
 struct HostTables {

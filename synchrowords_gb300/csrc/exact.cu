@@ -28,6 +28,7 @@
 #include "algos.cuh"
 #include "exact.hpp"
 #include "kernels.cuh"
+#include "learn.hpp"
 
 namespace sw {
 
@@ -68,6 +69,7 @@ class Engine {
     SW_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     pinned.reserve(4096);
     SW_CUDA(cudaMalloc(&d_misc, 64 * sizeof(u32)));
+    mlp = std::make_unique<MlpRunner>(stream);
   }
   ~Engine() {
     for (auto e : ev_pool) cudaEventDestroy(e);
@@ -78,6 +80,7 @@ class Engine {
 
   cudaStream_t stream = nullptr;
   HostPinned pinned;
+  std::unique_ptr<MlpRunner> mlp;
 
   // ---- optional per-kernel-class timing (CUDA events on `stream`) ----
   // class 0: subset-query tree walks, 1: layer expansion, 2: radix sorts,
@@ -1323,6 +1326,323 @@ void Solver::reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, 
   b.lower = b.lower > mlsw ? b.lower - mlsw : 0;
   b.upper -= mlsw;
   done();
+}
+
+// ---------------------------------------------------------------------------
+// Learned distance model: training pairs, scoring, training, learned beam.
+// ---------------------------------------------------------------------------
+namespace {
+// 8-word reference layout (state q = bit q % 64 of word q / 64) <-> device rows
+// of W words.
+std::vector<u64> ref8_to_rows(const uint64_t* ref, uint64_t count, uint32_t n, int W) {
+  std::vector<u64> out((size_t)count * W, 0);
+  for (uint64_t i = 0; i < count; ++i)
+    for (int w = 0; w < 8; ++w) {
+      uint64_t v = ref[i * 8 + w];
+      while (v) {
+        const int q = w * 64 + __builtin_ctzll(v);
+        v &= v - 1;
+        if ((uint32_t)q < n) out[(size_t)i * W + (q >> 6)] |= state_bit(q);
+      }
+    }
+  return out;
+}
+void rows_to_ref8(const u64* rows, uint64_t count, uint32_t n, int W, uint64_t* out) {
+  for (uint64_t i = 0; i < count; ++i) {
+    for (int w = 0; w < 8; ++w) out[i * 8 + w] = 0;
+    for (uint32_t q = 0; q < n; ++q)
+      if (rows[(size_t)i * W + (q >> 6)] & state_bit((int)q)) out[i * 8 + (q >> 6)] |= 1ULL << (q & 63);
+  }
+}
+}  // namespace
+
+void Solver::set_model(const float* params) {
+  SW_CUDA(cudaSetDevice(device_));
+  eng_->mlp->set_params(params);
+}
+void Solver::get_model(float* params) {
+  if (!eng_->mlp->has_params()) throw std::runtime_error("no distance model loaded");
+  SW_CUDA(cudaSetDevice(device_));
+  eng_->mlp->get_params(params);
+}
+bool Solver::has_model() const { return eng_->mlp->has_params(); }
+
+uint32_t Solver::distance_pairs(const Automaton& A, uint32_t per_layer, uint64_t max_inverse_sets,
+                                std::vector<uint64_t>& sets, std::vector<float>& labels,
+                                std::vector<uint32_t>& depths) {
+  sets.clear();
+  labels.clear();
+  depths.clear();
+  if (A.n < 2 || per_layer == 0) return 0;
+  // the reset length bounds the depths worth labelling
+  Bounds b;
+  b.upper = std::max<u64>(1, (u64)A.n * A.n * A.n / 6);
+  sw_exact_config cfg{1, 1, 0, 2048, 10000, (uint64_t)A.n * 16};
+  sw_stats st0{};
+  exact(A, cfg, b, st0);
+  if (b.non_synchro || b.lower != b.upper) return 0;
+  const u64 L = b.upper;
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  const int n = (int)A.n, k = (int)A.k, W = words_for(n);
+  E.upload_tables(A);
+  // inverse layers (complements of the maximal preimage sets), depth 0..D
+  E.B.reset();
+  std::vector<uint32_t> seeds = backward_seeds(A);
+  if (seeds.empty()) return 0;
+  {
+    std::vector<u64> rows((size_t)W * seeds.size(), 0);
+    for (size_t i = 0; i < seeds.size(); ++i)
+      for (int q = 0; q < n; ++q)
+        if ((uint32_t)q != seeds[i]) rows[i * W + (q >> 6)] |= state_bit(q);
+    E.B.rows.reserve(sizeof(u64) * rows.size());
+    E.B.vis.reserve(sizeof(u64) * rows.size());
+    SW_CUDA(cudaMemcpyAsync(E.B.rows.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+    SW_CUDA(cudaMemcpyAsync(E.B.vis.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+    E.B.count = E.B.vis_count = (u32)seeds.size();
+    E.sort_by_layer_key(W, E.B.vis.as<u64>(), E.B.vis_count);
+  }
+  std::vector<std::unique_ptr<DevBuf>> inv;
+  std::vector<u32> inv_count;
+  u64 inv_total = 0;
+  auto keep_layer = [&] {
+    inv.push_back(std::make_unique<DevBuf>());
+    inv.back()->reserve(sizeof(u64) * W * std::max<u32>(E.B.count, 1));
+    SW_CUDA(cudaMemcpyAsync(inv.back()->p, E.B.rows.p, sizeof(u64) * W * E.B.count, cudaMemcpyDeviceToDevice,
+                            E.stream));
+    inv_count.push_back(E.B.count);
+    inv_total += E.B.count;
+  };
+  keep_layer();
+  for (u64 j = 1; j <= L && inv_total < max_inverse_sets; ++j) {
+    E.step(E.B, false, W, n, k, true);
+    if (!E.B.count) break;
+    keep_layer();
+  }
+  const u32 D = (u32)inv.size() - 1;
+  // forward layers, sampled and labelled
+  E.F.reset();
+  {
+    std::vector<u64> full(W, 0);
+    for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
+    E.F.rows.reserve(sizeof(u64) * W);
+    E.F.vis.reserve(sizeof(u64) * W);
+    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
+    SW_CUDA(cudaMemcpyAsync(E.F.vis.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
+    E.F.count = E.F.vis_count = 1;
+  }
+  DevBuf idx_d, sample, flags;
+  for (u64 i = 0; i <= L; ++i) {
+    const u32 c = E.F.count;
+    const u32 s = std::min<u32>(c, per_layer);
+    std::vector<u32> idx(s);
+    for (u32 t = 0; t < s; ++t) idx[t] = (u32)(((u64)t * c) / s);
+    idx_d.reserve(sizeof(u32) * s);
+    sample.reserve(sizeof(u64) * W * s);
+    flags.reserve(sizeof(u32) * s);
+    SW_CUDA(cudaMemcpyAsync(idx_d.p, idx.data(), sizeof(u32) * s, cudaMemcpyHostToDevice, E.stream));
+    launch_gather_rows(W, E.F.rows.as<u64>(), idx_d.as<u32>(), s, sample.as<u64>(), E.stream);
+    std::vector<float> lab(s, (float)(D + 1));
+    std::vector<u32> fl(s);
+    u32 open = s;
+    for (u32 j = 0; j <= D && open; ++j) {
+      launch_fill_u32(flags.as<u32>(), 0, s, E.stream);
+      E.query(W, kQueryDisjoint, inv[j]->as<u64>(), inv_count[j], sample.as<u64>(), s, n, flags.as<u32>(), false);
+      SW_CUDA(cudaMemcpyAsync(fl.data(), flags.p, sizeof(u32) * s, cudaMemcpyDeviceToHost, E.stream));
+      SW_CUDA(cudaStreamSynchronize(E.stream));
+      for (u32 t = 0; t < s; ++t)
+        if (fl[t] && lab[t] > (float)j) {
+          lab[t] = (float)j;
+          --open;
+        }
+    }
+    std::vector<u64> rows((size_t)s * W);
+    SW_CUDA(cudaMemcpy(rows.data(), sample.p, sizeof(u64) * W * s, cudaMemcpyDeviceToHost));
+    const size_t base = sets.size();
+    sets.resize(base + (size_t)s * 8);
+    rows_to_ref8(rows.data(), s, (uint32_t)n, W, sets.data() + base);
+    labels.insert(labels.end(), lab.begin(), lab.end());
+    depths.insert(depths.end(), s, (uint32_t)i);
+    if (i == L) break;
+    E.step(E.F, true, W, n, k, true);
+    if (!E.F.count) break;
+  }
+  return (uint32_t)L;
+}
+
+void Solver::mlp_forward(const Automaton& A, const uint64_t* sets, uint64_t count, float* out) {
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  if (!count) return;
+  const std::vector<u64> rows = ref8_to_rows(sets, count, A.n, 8);
+  DevBuf d_rows, d_y;
+  d_rows.reserve(sizeof(u64) * rows.size());
+  d_y.reserve(sizeof(float) * count);
+  SW_CUDA(cudaMemcpyAsync(d_rows.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+  E.mlp->prepare(A);
+  E.mlp->forward(d_rows.as<u64>(), 8, (u32)count, d_y.as<float>());
+  SW_CUDA(cudaMemcpyAsync(out, d_y.p, sizeof(float) * count, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+}
+
+float Solver::mlp_gradient(const Automaton& A, const uint64_t* sets, const float* labels, uint64_t count,
+                           float* grad) {
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  if (!count) throw std::invalid_argument("empty batch");
+  const std::vector<u64> rows = ref8_to_rows(sets, count, A.n, 8);
+  DevBuf d_rows, d_y, d_t;
+  d_rows.reserve(sizeof(u64) * rows.size());
+  d_y.reserve(sizeof(float) * count);
+  d_t.reserve(sizeof(float) * count);
+  SW_CUDA(cudaMemcpyAsync(d_rows.p, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice, E.stream));
+  SW_CUDA(cudaMemcpyAsync(d_t.p, labels, sizeof(float) * count, cudaMemcpyHostToDevice, E.stream));
+  E.mlp->prepare(A);
+  E.mlp->zero_grad();
+  E.mlp->forward(d_rows.as<u64>(), 8, (u32)count, d_y.as<float>());
+  E.mlp->backward(d_t.as<float>(), (u32)count);
+  float loss = 0;
+  SW_CUDA(cudaMemcpyAsync(grad, E.mlp->grad(), sizeof(float) * mlp::kParams, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaMemcpyAsync(&loss, E.mlp->loss(), sizeof(float), cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaStreamSynchronize(E.stream));
+  return loss;
+}
+
+float Solver::mlp_train(const std::vector<Automaton>& autos, const uint64_t* offsets, const uint64_t* sets,
+                        const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed) {
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  const size_t A_n = autos.size();
+  const uint64_t total = offsets[A_n];
+  if (!total || !batch) throw std::invalid_argument("no training pairs");
+  // all pairs resident on the device as 8-word rows
+  DevBuf d_rows, d_lab, d_y;
+  d_rows.reserve(sizeof(u64) * 8 * total);
+  d_lab.reserve(sizeof(float) * total);
+  d_y.reserve(sizeof(float) * batch);
+  for (size_t a = 0; a < A_n; ++a) {
+    const uint64_t o = offsets[a], c = offsets[a + 1] - o;
+    if (!c) continue;
+    const std::vector<u64> rows = ref8_to_rows(sets + o * 8, c, autos[a].n, 8);
+    SW_CUDA(cudaMemcpy(d_rows.as<u64>() + o * 8, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice));
+  }
+  SW_CUDA(cudaMemcpy(d_lab.p, labels, sizeof(float) * total, cudaMemcpyHostToDevice));
+  std::vector<size_t> order(A_n);
+  for (size_t a = 0; a < A_n; ++a) order[a] = a;
+  uint64_t state = seed;
+  auto next = [&] {  // SplitMix64
+    uint64_t z = (state += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+  };
+  double last = 0;
+  for (uint32_t ep = 0; ep < epochs; ++ep) {
+    for (size_t a = A_n; a > 1; --a) std::swap(order[a - 1], order[next() % a]);
+    double sum = 0;
+    uint64_t steps = 0;
+    for (size_t oi = 0; oi < A_n; ++oi) {
+      const size_t a = order[oi];
+      for (uint64_t o = offsets[a]; o < offsets[a + 1]; o += batch) {
+        const u32 c = (u32)std::min<uint64_t>(batch, offsets[a + 1] - o);
+        E.mlp->prepare(autos[a]);
+        E.mlp->zero_grad();
+        E.mlp->forward(d_rows.as<u64>() + o * 8, 8, c, d_y.as<float>());
+        E.mlp->backward(d_lab.as<float>() + o, c);
+        E.mlp->adam_step(lr);
+        float l = 0;
+        SW_CUDA(cudaMemcpyAsync(&l, E.mlp->loss(), sizeof(float), cudaMemcpyDeviceToHost, E.stream));
+        SW_CUDA(cudaStreamSynchronize(E.stream));
+        sum += l;
+        ++steps;
+      }
+    }
+    last = steps ? sum / steps : 0.0;
+  }
+  return (float)last;
+}
+
+void Solver::learned_beam(const Automaton& A, const sw_learned_beam_config& cfg, Bounds& b, sw_stats& st) {
+  if (b.non_synchro || b.lower == b.upper) return;
+  const bool use_model = cfg.order != SW_ORDER_SIZE;
+  if (use_model && !has_model()) throw std::runtime_error("LearnedBeam: no distance model loaded");
+  if (A.n == 1) {
+    b.lower = b.upper = 0;
+    b.has_word = true;
+    b.word.clear();
+    return;
+  }
+  SW_CUDA(cudaSetDevice(device_));
+  Engine& E = *eng_;
+  E.st = &st;
+  auto t0 = std::chrono::steady_clock::now();
+  const int n = (int)A.n, k = (int)A.k, W = words_for(n);
+  E.upload_tables(A);
+  if (use_model) E.mlp->prepare(A);
+  E.F.reset();
+  {
+    std::vector<u64> full(W, 0);
+    for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
+    E.F.rows.reserve(sizeof(u64) * W);
+    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, full.data(), sizeof(u64) * W, cudaMemcpyHostToDevice, E.stream));
+    E.F.count = 1;
+    E.F.vis_count = 0;
+  }
+  const u32 width = (u32)std::min<uint64_t>(cfg.beam_size, 1u << 26);
+  DevBuf counts, scores, keys, vals, alt_k, alt_v, sel_rows, sel_origin;
+  std::vector<u32> pc;
+  u64 found_len = 0;
+  std::vector<uint32_t> word;
+  for (u64 depth = 1; depth < b.upper && (cfg.max_iter < 0 || depth <= (u64)cfg.max_iter); ++depth) {
+    E.step(E.F, true, W, n, k, /*dominance=*/false);  // children, duplicates removed, origins recorded
+    const u32 m = E.F.count;
+    if (!m) break;
+    counts.reserve(sizeof(u32) * m);
+    launch_popcount(W, E.F.rows.as<u64>(), m, counts.as<u32>(), E.stream);
+    pc.resize(m);
+    SW_CUDA(cudaMemcpyAsync(pc.data(), counts.p, sizeof(u32) * m, cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaStreamSynchronize(E.stream));
+    u32 hit = UINT32_MAX;
+    for (u32 i = 0; i < m && hit == UINT32_MAX; ++i)
+      if (pc[i] == 1) hit = i;
+    if (hit != UINT32_MAX) {
+      word = E.trace(E.F, hit, nullptr);
+      std::reverse(word.begin(), word.end());
+      found_len = depth;
+      break;
+    }
+    if (m <= width) continue;
+    // keep the `width` children with the smallest score (ties: child order)
+    keys.reserve(sizeof(u64) * m);
+    vals.reserve(sizeof(u32) * m);
+    if (use_model) {
+      scores.reserve(sizeof(float) * m);
+      E.mlp->forward(E.F.rows.as<u64>(), W, m, scores.as<float>());
+    }
+    launch_score_keys(use_model ? scores.as<float>() : nullptr,
+                      cfg.order != SW_ORDER_MODEL ? counts.as<u32>() : nullptr, m, keys.as<u64>(), E.stream);
+    launch_iota(vals.as<u32>(), m, E.stream);
+    E.sort_rows(1, keys.as<u64>(), vals.as<u32>(), m);
+    sel_rows.reserve(sizeof(u64) * W * width);
+    sel_origin.reserve(sizeof(u32) * width);
+    launch_gather_rows(W, E.F.rows.as<u64>(), vals.as<u32>(), width, sel_rows.as<u64>(), E.stream);
+    Layer& top = *E.F.layers.back();
+    launch_gather_u32(top.origin.as<u32>(), vals.as<u32>(), width, sel_origin.as<u32>(), E.stream);
+    SW_CUDA(cudaMemcpyAsync(E.F.rows.p, sel_rows.p, sizeof(u64) * W * width, cudaMemcpyDeviceToDevice, E.stream));
+    SW_CUDA(cudaMemcpyAsync(top.origin.p, sel_origin.p, sizeof(u32) * width, cudaMemcpyDeviceToDevice, E.stream));
+    top.count = width;
+    E.F.count = width;
+    E.count_launch(5);
+  }
+  if (found_len && found_len < b.upper) {
+    if (apply_word(A, word).size() != 1 || word.size() != found_len)
+      throw std::runtime_error("internal: learned beam word does not synchronize");
+    b.upper = found_len;
+    b.has_word = true;
+    b.word = word;
+  }
+  st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  E.st = nullptr;
 }
 
 }  // namespace sw

@@ -54,6 +54,21 @@ class Solver {
   // Brute::run semantics (power-set BFS, n <= 32): exact length and a word.
   void brute(const Automaton& A, const sw_brute_config& cfg, Bounds& b, sw_stats& st);
 
+  // Forward beam scored by the loaded distance model (or by set size).
+  void learned_beam(const Automaton& A, const sw_learned_beam_config& cfg, Bounds& b, sw_stats& st);
+
+  // Learned distance model (sets in the 8-word reference layout).
+  void set_model(const float* params);
+  void get_model(float* params);
+  bool has_model() const;
+  // Labelled forward-layer sets; returns the reset length (0 if none found).
+  uint32_t distance_pairs(const Automaton& A, uint32_t per_layer, uint64_t max_inverse_sets,
+                          std::vector<uint64_t>& sets, std::vector<float>& labels, std::vector<uint32_t>& depths);
+  void mlp_forward(const Automaton& A, const uint64_t* sets, uint64_t count, float* out);
+  float mlp_gradient(const Automaton& A, const uint64_t* sets, const float* labels, uint64_t count, float* grad);
+  float mlp_train(const std::vector<Automaton>& autos, const uint64_t* offsets, const uint64_t* sets,
+                  const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed);
+
   // Kernel-level helpers (reference bitset layout on the host).
   void apply_transition(const Automaton& A, uint32_t letter, bool inverse, const uint64_t* from, uint64_t* to,
                         uint64_t count);

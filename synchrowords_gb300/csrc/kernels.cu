@@ -919,13 +919,16 @@ __global__ void k_score_keys(const float* __restrict__ score, const u32* __restr
                              u64* __restrict__ keys) {
   const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
-  u32 u;
+  u32 s = 0;
   if (score) {
-    u = __float_as_uint(score[i]);
-    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);  // IEEE order -> unsigned order
-  } else {
-    u = counts[i];
+    s = __float_as_uint(score[i]);
+    s = (s & 0x80000000u) ? ~s : (s | 0x80000000u);  // IEEE order -> unsigned order
   }
+  u32 u;
+  if (score && counts)
+    u = (counts[i] << 16) | (s >> 16);  // size first, then the score's leading 16 bits
+  else
+    u = score ? s : counts[i];
   keys[i] = ((u64)u << 32) | i;
 }
 

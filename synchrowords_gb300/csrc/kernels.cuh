@@ -110,8 +110,9 @@ void launch_beam_keys(int W, const u64* rows, u32 m, int n, int R, u64* keys, cu
 // dst[i] = src[idx[i]] (u32 payloads).
 void launch_gather_u32(const u32* src, const u32* idx, u32 m, u32* dst, cudaStream_t s);
 
-// Ascending sort keys of beam candidates: keys[i] = (order-preserving bits of
-// score[i]) << 32 | i, from float scores or (when score is null) u32 counts.
+// Ascending sort keys of beam candidates: keys[i] = primary << 32 | i with
+// primary = the order-preserving bits of score[i] (counts null), counts[i]
+// (score null), or counts[i] << 16 | leading 16 bits of score[i] (both).
 void launch_score_keys(const float* score, const u32* counts, u32 m, u64* keys, cudaStream_t s);
 
 // Fill u32 array with a value.

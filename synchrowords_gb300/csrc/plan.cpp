@@ -799,6 +799,25 @@ void plan_from_json(const std::string& text, uint32_t n, uint32_t k, sw_plan* ou
       alg.kind = SW_ALGO_REDUCE;
       alg.reduce.min_n = value_of(cfg, "min_n", "80", n, k).as_u64();
       alg.reduce.list_size_threshold = value_of(cfg, "list_size_threshold", "AUT_N * 16", n, k).as_u64();
+    } else if (name == "LearnedBeam") {  // no reference counterpart
+      alg.kind = SW_ALGO_LEARNED_BEAM;
+      alg.learned_beam.beam_size = value_of(cfg, "beam_size", "4096", n, k).as_u64();
+      alg.learned_beam.max_iter = value_of(cfg, "max_iter", "-1", n, k).as_i64();
+      std::string order = "model";
+      if (cfg && cfg->get("order")) {
+        const Json* o = cfg->get("order");
+        if (o->type != Json::String) throw std::runtime_error("order value not in [model, size, size_model]");
+        order = o->str;
+      }
+      if (order == "model")
+        alg.learned_beam.order = SW_ORDER_MODEL;
+      else if (order == "size")
+        alg.learned_beam.order = SW_ORDER_SIZE;
+      else if (order == "size_model")
+        alg.learned_beam.order = SW_ORDER_SIZE_MODEL;
+      else
+        throw std::runtime_error("order value not in [model, size, size_model]");
+      if (alg.learned_beam.beam_size == 0) throw std::runtime_error("LearnedBeam: beam_size must be positive");
     } else {
       throw std::runtime_error("Unknown algorithm: " + name);  // synchrolib.hpp:205
     }
