@@ -214,6 +214,11 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     workers = std::max<uint32_t>(1, std::min<uint32_t>(workers, count));
     while (ctx->workers.size() + 1 < workers)
       ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
+    if (ctx->solver->has_model()) {  // every worker scores with the context's distance model
+      std::vector<float> model(SW_MLP_PARAMS);
+      ctx->solver->get_model(model.data());
+      for (uint32_t w = 1; w < workers; ++w) ctx->workers[w - 1]->set_model(model.data());
+    }
     std::atomic<uint32_t> next{0};
     std::atomic<int> first_rc{SW_OK};
     std::mutex err_mu;

@@ -2,6 +2,8 @@
 // app/args.hpp:51-78 and app/io.hpp:95-142), driving the GPU library through
 // its C ABI.  Same flags, input format and output line; no JIT step: one
 // binary serves every (n, k).
+#include <unistd.h>
+
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -41,7 +43,7 @@ void log(int level, const std::string& msg) {
 }
 
 struct Args {
-  std::string input, config, output, suffix;
+  std::string input, config, output, suffix, model;
   bool has_output = false, verbose = false, quiet = false, debug = false, cont = false;
 };
 
@@ -58,6 +60,8 @@ void usage() {
       "  -v, --verbose           Verbose output\n"
       "  -q, --quiet             Quiet output (only warnings and errors)\n"
       "  -d, --debug             Debug output (all messages and timers)\n"
+      "  -m, --model arg         Distance model for LearnedBeam (default: the packaged\n"
+      "                          ../models/distance_mlp.f32 beside this program, if present)\n"
       "  -h, --help              Print usage\n");
 }
 
@@ -86,6 +90,8 @@ Args parse(int argc, char** argv) {
       a.has_output = true;
     } else if (s == "-b" || s.rfind("--build-suffix", 0) == 0) {
       a.suffix = value("build-suffix");
+    } else if (s == "-m" || s.rfind("--model", 0) == 0) {
+      a.model = value("model");
     } else if (s == "--continue") {
       a.cont = true;
     } else if (s == "-v" || s == "--verbose") {
@@ -174,6 +180,30 @@ int main(int argc, char** argv) {
 
   sw_context* ctx = nullptr;
   if (sw_context_create(0, &ctx) != SW_OK) die(std::string("GPU unavailable: ") + sw_last_error(), 4);
+  {
+    // the distance model LearnedBeam ranks by: --model, else the packaged one
+    std::string path = args.model;
+    if (path.empty()) {
+      char exe[4096];
+      const ssize_t len = readlink("/proc/self/exe", exe, sizeof exe - 1);
+      if (len > 0) {
+        exe[len] = 0;
+        std::string dir(exe);
+        dir = dir.substr(0, dir.rfind('/'));
+        path = dir + "/../models/distance_mlp.f32";
+      }
+    }
+    std::ifstream mf(path, std::ios::binary);
+    if (mf) {
+      std::vector<float> params(SW_MLP_PARAMS);
+      mf.read(reinterpret_cast<char*>(params.data()), sizeof(float) * params.size());
+      if (mf.gcount() != (std::streamsize)(sizeof(float) * params.size()))
+        die("Model file " + path + " does not hold " + std::to_string(SW_MLP_PARAMS) + " floats", 1);
+      if (sw_context_set_model(ctx, params.data(), SW_MLP_PARAMS) != SW_OK) die(sw_last_error(), 4);
+    } else if (!args.model.empty()) {
+      die("Error while opening the model file", 1);
+    }
+  }
 
   size_t index = 0;
   for (const auto& a : auts) {

@@ -132,6 +132,16 @@ def test_learned_beam_bound_feeds_exact(ctx):
         assert len(oracle.apply_word(d, n, 2, r.word)) == 1
 
 
+def test_batch_workers_use_the_context_model(ctx):
+    if not sw.DEFAULT_MODEL.exists():
+        pytest.skip("no packaged model")
+    autos = [(100, 2, random_dfa(100, 2, 70 + i)) for i in range(6)]
+    res = ctx.solve_batch(autos, plan(("LearnedBeam", {}), ("Exact", {})), workers=3)
+    for (n, k, d), r in zip(autos, res):
+        assert r.lower == r.upper == oracle.exact(d, n, k).upper
+        assert len(oracle.apply_word(d, n, k, r.word)) == 1
+
+
 def test_size_ordered_beam_without_a_model(ctx):
     # order "size" needs no model: the beam keeps the smallest children
     c = sw.Context(0, model=None)

@@ -82,3 +82,34 @@ def test_algorithms_after_reduce_leave_bounds_alone(ctx):
     plan["algorithms"].append({"name": "Exact", "config": {}})
     r = ctx.solve(d, c["n"], c["k"], json.dumps(plan))
     assert r.lower == r.upper == 18
+
+
+def test_cli_readme_run_and_learned_beam(tmp_path):
+    """The `synchro` drop-in on the README input and plan (expected lines of
+    docs/install.md:101-104), then a plan with LearnedBeam, which ranks by the
+    packaged distance model the program finds beside itself."""
+    import subprocess
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    cli = root / "synchrowords_gb300" / "_build" / "synchro"
+    g = json.loads((GOLD / "readme.json").read_text())
+    (tmp_path / "in.txt").write_text("".join(f"{a['k']} {a['n']}\n" + " ".join(map(str, a["delta"])) + "\n"
+                                             for a in g["automata"]))
+    (tmp_path / "plan.json").write_text(json.dumps(README_PLAN))
+    r = subprocess.run([str(cli), "-f", str(tmp_path / "in.txt"), "-c", str(tmp_path / "plan.json"), "-o",
+                        str(tmp_path / "out.txt"), "-q"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = (tmp_path / "out.txt").read_text().splitlines()
+    assert lines[1] == "1: NON SYNCHRO"
+    for i, exp in enumerate(g["expected"]):
+        if "lower" in exp:
+            assert lines[i].startswith(f"{i}: [{exp['lower']}, {exp['upper']}] ((Brute, ")
+    learned = {"algorithms": [{"name": "LearnedBeam", "config": {}}, {"name": "Exact", "config": {}}]}
+    (tmp_path / "learned.json").write_text(json.dumps(learned))
+    r = subprocess.run([str(cli), "-f", str(tmp_path / "in.txt"), "-c", str(tmp_path / "learned.json"), "-q",
+                        "-o", str(tmp_path / "learned.txt")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert (tmp_path / "learned.txt").read_text().splitlines()[3].startswith("3: [18, 18] ((LearnedBeam, ")
+    r = subprocess.run([str(cli), "-f", str(tmp_path / "in.txt"), "-c", str(tmp_path / "learned.json"), "-q",
+                        "-m", str(tmp_path / "missing.f32")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 1
