@@ -251,6 +251,15 @@ class Engine {
   // One BFS layer on side X (forward = image, backward = preimage of complements).
   // With `dominance` false only duplicates are removed and the visited list is
   // left alone (the bounded inverse phase, see Solver::exact).
+  // Drop children with a proper subset in their own layer (the reference's
+  // self reduction).  Solver::exact turns it off while it cannot pay: it
+  // shrinks a layer by ~15% at the cost of a layer-by-layer subset query,
+  // which repays itself only when the lists are large or feed the bounded
+  // phase (measured: n = 200 plain Exact 7.4 vs 10.3 ms per DFA without it;
+  // n = 320 Beam+Exact 949 vs 863 ms with it).  Lengths are the same
+  // either way: the visited check and the meet check do not depend on it.
+  bool self_check = true;
+
   void step(Side& X, bool forward, int W, int n, int k, bool dominance = true) {
     const u32 m = X.count;
     const u64 N = (u64)m * k;
@@ -311,8 +320,9 @@ class Engine {
       query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, uq_rows.as<u64>(), u, n,
             flags_a.as<u32>(), false);
     const double t_vis = vclock();
-    query(W, kQueryProperSubset, uq_rows.as<u64>(), u, uq_rows.as<u64>(), u, n,
-          flags_b.as<u32>(), false);
+    if (self_check)
+      query(W, kQueryProperSubset, uq_rows.as<u64>(), u, uq_rows.as<u64>(), u, n,
+            flags_b.as<u32>(), false);
     const double t_self = vclock();
     if (verbose) {
       std::vector<u32> fa(u), fb(u);
@@ -698,6 +708,10 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     }
     rt++;
     const u32 parents_before = X.count;
+    // self reduction only where it pays: a word-backed bound (the bounded
+    // phase expands B from its size at the switch) or lists past a quarter
+    // of the memory budget
+    E.self_check = b.has_word || 4 * (live + next) > budget;
     E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
     // projected branching of the bounded levels: distinct children per parent
     // before pruning, never below 1.5, plus 10% margin
@@ -1202,6 +1216,7 @@ void Solver::reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, 
   auto t0 = std::chrono::steady_clock::now();
   const int n = (int)A.n, k = (int)A.k, W = words_for(n);
   E.upload_tables(A);
+  E.self_check = true;  // the reference's step (reduce.hpp:186-187): its list sizes decide the reduction
   E.F.reset();
   std::vector<u64> full(W, 0);
   for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
@@ -1386,6 +1401,7 @@ uint32_t Solver::distance_pairs(const Automaton& A, uint32_t per_layer, uint64_t
   Engine& E = *eng_;
   const int n = (int)A.n, k = (int)A.k, W = words_for(n);
   E.upload_tables(A);
+  E.self_check = true;  // labelled layers are the fully reduced ones
   // inverse layers (complements of the maximal preimage sets), depth 0..D
   E.B.reset();
   std::vector<uint32_t> seeds = backward_seeds(A);
