@@ -251,14 +251,19 @@ class Engine {
   // One BFS layer on side X (forward = image, backward = preimage of complements).
   // With `dominance` false only duplicates are removed and the visited list is
   // left alone (the bounded inverse phase, see Solver::exact).
-  // Drop children with a proper subset in their own layer (the reference's
-  // self reduction).  Solver::exact turns it off while it cannot pay: it
-  // shrinks a layer by ~15% at the cost of a layer-by-layer subset query,
-  // which repays itself only when the lists are large or feed the bounded
-  // phase (measured: n = 200 plain Exact 7.4 vs 10.3 ms per DFA without it;
-  // n = 320 Beam+Exact 949 vs 863 ms with it).  Lengths are the same
-  // either way: the visited check and the meet check do not depend on it.
+  // Dominance reductions (the reference's self and visited reductions).
+  // self_check: drop children with a proper subset in their own layer;
+  // visited_subsets: drop children containing a visited set (false: only
+  // children equal to a visited set, by a sorted-membership search).
+  // Solver::exact runs the full reductions only where they pay: each removes
+  // ~15% of a layer for a layer-by-layer subset query, which repays itself
+  // when the lists are large or feed the bounded phase.  Measured (ms per
+  // DFA): n = 200 plain Exact 4.8 with duplicates only, 7.3 with the visited
+  // subset check, 10.3 with both reductions; n = 320 Beam+Exact 949 without
+  // the self reduction, 863 with both.  Lengths are the same either way:
+  // every kept set is still a set of its layer and the meet check is exact.
   bool self_check = true;
+  bool visited_subsets = true;
 
   void step(Side& X, bool forward, int W, int n, int k, bool dominance = true) {
     const u32 m = X.count;
@@ -316,9 +321,17 @@ class Engine {
     launch_fill_u32(flags_b.as<u32>(), 0, u, stream);
     count_launch(2);
     const double t_sort = vclock();
-    if (X.vis_count)
-      query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, uq_rows.as<u64>(), u, n,
-            flags_a.as<u32>(), false);
+    if (X.vis_count) {
+      if (visited_subsets) {
+        query(W, kQuerySubset, X.vis.as<u64>(), X.vis_count, uq_rows.as<u64>(), u, n, flags_a.as<u32>(), false);
+      } else {
+        timed(3, (double)u * 8.0 * W, [&] {
+          launch_member_key(W, X.vis.as<u64>(), X.vis_count, uq_rows.as<u64>(), u, flags_a.as<u32>(), stream,
+                            X.keymap);
+        });
+        count_launch();
+      }
+    }
     const double t_vis = vclock();
     if (self_check)
       query(W, kQueryProperSubset, uq_rows.as<u64>(), u, uq_rows.as<u64>(), u, n,
@@ -711,7 +724,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     // self reduction only where it pays: a word-backed bound (the bounded
     // phase expands B from its size at the switch) or lists past a quarter
     // of the memory budget
-    E.self_check = b.has_word || 4 * (live + next) > budget;
+    E.self_check = E.visited_subsets = b.has_word || 4 * (live + next) > budget;
     E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
     // projected branching of the bounded levels: distinct children per parent
     // before pruning, never below 1.5, plus 10% margin
@@ -1216,7 +1229,7 @@ void Solver::reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, 
   auto t0 = std::chrono::steady_clock::now();
   const int n = (int)A.n, k = (int)A.k, W = words_for(n);
   E.upload_tables(A);
-  E.self_check = true;  // the reference's step (reduce.hpp:186-187): its list sizes decide the reduction
+  E.self_check = E.visited_subsets = true;  // the reference's step (reduce.hpp:186-187): its list sizes decide the reduction
   E.F.reset();
   std::vector<u64> full(W, 0);
   for (int q = 0; q < n; ++q) full[q >> 6] |= state_bit(q);
@@ -1401,7 +1414,7 @@ uint32_t Solver::distance_pairs(const Automaton& A, uint32_t per_layer, uint64_t
   Engine& E = *eng_;
   const int n = (int)A.n, k = (int)A.k, W = words_for(n);
   E.upload_tables(A);
-  E.self_check = true;  // labelled layers are the fully reduced ones
+  E.self_check = E.visited_subsets = true;  // labelled layers are the fully reduced ones
   // inverse layers (complements of the maximal preimage sets), depth 0..D
   E.B.reset();
   std::vector<uint32_t> seeds = backward_seeds(A);

@@ -819,6 +819,44 @@ void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* ou
   SW_LAUNCH_CHECK();
 }
 
+// flags[i] = 1 when row i of C equals some row of V (both sorted by the same
+// layer key): a binary search for C's key in V, then a scan of V's rows with
+// that key.
+template <int W>
+__global__ void k_member_key(const u64* __restrict__ V, u32 nv, const u64* __restrict__ C, u32 nc, KeyMap map,
+                             u32* __restrict__ flags) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc) return;
+  const u64* x = C + (size_t)i * W;
+  u64 x0, x1;
+  layer_key<W>(x, map, x0, x1);
+  u32 lo = 0, hi = nv;
+  while (lo < hi) {
+    const u32 mid = (lo + hi) >> 1;
+    u64 y0, y1;
+    layer_key<W>(V + (size_t)mid * W, map, y0, y1);
+    if (y0 < x0 || (y0 == x0 && y1 < x1)) lo = mid + 1;
+    else hi = mid;
+  }
+  for (u32 j = lo; j < nv; ++j) {
+    const u64* y = V + (size_t)j * W;
+    u64 y0, y1;
+    layer_key<W>(y, map, y0, y1);
+    if (y0 != x0 || y1 != x1) break;
+    if (row_eq<W>(x, y)) {
+      flags[i] = 1u;
+      return;
+    }
+  }
+}
+
+void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
+                       const KeyMap& map) {
+  if (!nc || !nv) return;
+  SW_DISPATCH_W(W, (k_member_key<WW><<<(nc + 255) / 256, 256, 0, s>>>(V, nv, C, nc, map, flags)));
+  SW_LAUNCH_CHECK();
+}
+
 // counts[q] += number of rows containing state q (block histograms in shared memory).
 template <int W>
 __global__ void k_state_counts(const u64* __restrict__ rows, u32 m, u32* __restrict__ counts) {

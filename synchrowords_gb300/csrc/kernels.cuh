@@ -95,6 +95,10 @@ void launch_layer_keys(int W, const u64* rows, u32 m, u64* keys, cudaStream_t s,
 // Merge of two row arrays sorted by the same layer key.
 void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s,
                       const KeyMap& map = KeyMap{});
+// flags[i] = 1 if row i of C equals a row of V (flags untouched otherwise);
+// V and C sorted by the same layer key.
+void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
+                       const KeyMap& map = KeyMap{});
 // counts[q] += rows containing state q (counts: 64*W entries, caller-zeroed).
 void launch_state_counts(int W, const u64* rows, u32 m, u32* counts, cudaStream_t s);
 
