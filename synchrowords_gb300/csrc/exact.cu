@@ -210,14 +210,13 @@ class Engine {
     alt_rows.reserve(sizeof(u64) * R * (size_t)m);
     alt_vals.reserve(sizeof(u32) * (size_t)m);
     sort_tmp.reserve(sort_temp_bytes(R, m));
-    int launches = 0;
+    int launches = 0, passes = 0;
     // algorithmic bytes: every pass reads and writes each (row, payload) once
-    // and the upsweep reads one digit word per row
     timed(2, 0.0, [&] {
-      launches = radix_sort_rows(R, rows, vals, alt_rows.as<u64>(), alt_vals.as<u32>(), m, sort_tmp.p, stream);
+      launches =
+          radix_sort_rows(R, rows, vals, alt_rows.as<u64>(), alt_vals.as<u32>(), m, sort_tmp.p, stream, &passes);
     });
-    const int passes = launches > 1 ? (launches - 1) / 5 : 1;
-    if (prof_on) prof[2].bytes += (double)m * passes * (8.0 + 2.0 * (8.0 * R + 4));
+    if (prof_on) prof[2].bytes += (double)m * passes * 2.0 * (8.0 * R + 4);
     count_launch(launches);
   }
 

@@ -299,6 +299,7 @@ namespace {
 constexpr int kRsThreads = 256;
 constexpr int kRsRounds = 8;
 constexpr u32 kRsTile = kRsThreads * kRsRounds;
+constexpr u32 kMergeSortMax = 1u << 20;  // up to here: chunk sorts + merge passes; above: radix passes
 
 template <int R>
 constexpr u32 small_sort_max() {
@@ -425,7 +426,12 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(const u64* __restri
 
 // Whole sort in one block, rows in shared memory (m <= small_sort_max<R>()).
 template <int R>
-__global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u32 m) {
+__global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u32 m_total, u32 chunk) {
+  // block b sorts rows [b * chunk, min(m_total, (b + 1) * chunk))
+  const u32 base = blockIdx.x * chunk;
+  const u32 m = min(chunk, m_total - base);
+  keys += (size_t)base * R;
+  vals += base;
   extern __shared__ u64 s_mem[];
   u64* ka = s_mem;
   u64* kb = ka + (size_t)m * R;
@@ -518,8 +524,46 @@ size_t sort_temp_bytes(int R, u32 m) {
   return 2 * counts + scan_temp_bytes(256 * ntiles) + 2 * sizeof(u64) * 16 + 256;
 }
 
+// One merge pass: sorted runs of `run` rows are merged pairwise.  Each row
+// finds its rank in the partner run by binary search (left-run rows count
+// partner keys strictly smaller, right-run rows count keys not greater, so the
+// merge is stable) and is written straight to its final place.
 template <int R>
-static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+__global__ void k_merge_runs(const u64* __restrict__ ki, const u32* __restrict__ vi, u32 m, u32 run,
+                             u64* __restrict__ ko, u32* __restrict__ vo) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const u32 r = i / run;
+  const u32 pair = (r & ~1u) * run;
+  const bool left = (r & 1u) == 0;
+  const u32 own = i - r * run;
+  const u32 pstart = left ? pair + run : pair;
+  const u32 plen = pstart >= m ? 0u : min(run, m - pstart);
+  u64 x[R];
+#pragma unroll
+  for (int w = 0; w < R; ++w) x[w] = ki[(size_t)i * R + w];
+  u32 lo = 0, hi = plen;
+  while (lo < hi) {
+    const u32 mid = (lo + hi) >> 1;
+    const u64* y = ki + (size_t)(pstart + mid) * R;
+    int cmp = 0;  // sign of y - x
+#pragma unroll
+    for (int w = 0; w < R; ++w)
+      if (cmp == 0 && y[w] != x[w]) cmp = y[w] < x[w] ? -1 : 1;
+    const bool before = left ? cmp < 0 : cmp <= 0;
+    if (before) lo = mid + 1;
+    else hi = mid;
+  }
+  const size_t out = (size_t)pair + own + lo;
+#pragma unroll
+  for (int w = 0; w < R; ++w) ko[out * R + w] = x[w];
+  vo[out] = vi[i];
+}
+
+template <int R>
+static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s,
+                             int* data_passes) {
+  if (data_passes) *data_passes = 0;
   if (m <= 1) return 0;
   if (m <= small_sort_max<R>()) {
     size_t smem = (size_t)m * (2 * R * sizeof(u64) + 2 * sizeof(u32));
@@ -530,9 +574,41 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
       const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
       SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
     });
-    k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m);
+    k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m, m);
     SW_LAUNCH_CHECK();
+    if (data_passes) *data_passes = 1;
     return 1;
+  }
+  if (m <= kMergeSortMax) {
+    // mid sizes: chunks sorted in shared memory by one block each, then
+    // pairwise merges of sorted runs (each a single launch), instead of a
+    // 3-launch pass per key digit
+    const u32 chunk = small_sort_max<R>();
+    const u32 nchunks = (m + chunk - 1) / chunk;
+    static std::once_flag once2;
+    std::call_once(once2, [] {
+      const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
+      SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
+    });
+    const size_t smem = (size_t)chunk * (2 * R * sizeof(u64) + 2 * sizeof(u32));
+    k_rs_small<R><<<nchunks, kRsThreads, smem, s>>>(keys, vals, m, chunk);
+    SW_LAUNCH_CHECK();
+    u64 *ki = keys, *ko = keys_alt;
+    u32 *vi = vals, *vo = vals_alt;
+    int merges = 0;
+    for (u32 run = chunk; run < m; run *= 2) {
+      k_merge_runs<R><<<(m + 255) / 256, 256, 0, s>>>(ki, vi, m, run, ko, vo);
+      SW_LAUNCH_CHECK();
+      std::swap(ki, ko);
+      std::swap(vi, vo);
+      ++merges;
+    }
+    if (ki != keys) {
+      SW_CUDA(cudaMemcpyAsync(keys, ki, sizeof(u64) * R * (size_t)m, cudaMemcpyDeviceToDevice, s));
+      SW_CUDA(cudaMemcpyAsync(vals, vi, sizeof(u32) * (size_t)m, cudaMemcpyDeviceToDevice, s));
+    }
+    if (data_passes) *data_passes = 1 + merges;
+    return 1 + merges;
   }
   const u32 ntiles = (m + kRsTile - 1) / kRsTile;
   char* t = static_cast<char*>(temp);
@@ -570,20 +646,22 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
     SW_CUDA(cudaMemcpyAsync(keys, ki, sizeof(u64) * R * (size_t)m, cudaMemcpyDeviceToDevice, s));
     SW_CUDA(cudaMemcpyAsync(vals, vi, sizeof(u32) * (size_t)m, cudaMemcpyDeviceToDevice, s));
   }
+  if (data_passes) *data_passes = passes;
   return 1 + 5 * passes;  // or/and reduction + (upsweep, 3 scan kernels, downsweep) per pass
 }
 
-int radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s) {
+int radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp, cudaStream_t s,
+                    int* data_passes) {
   switch (R) {
-    case 1: return radix_sort_rows_t<1>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 2: return radix_sort_rows_t<2>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 3: return radix_sort_rows_t<3>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 4: return radix_sort_rows_t<4>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 5: return radix_sort_rows_t<5>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 6: return radix_sort_rows_t<6>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 7: return radix_sort_rows_t<7>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 8: return radix_sort_rows_t<8>(keys, vals, keys_alt, vals_alt, m, temp, s);
-    case 9: return radix_sort_rows_t<9>(keys, vals, keys_alt, vals_alt, m, temp, s);
+    case 1: return radix_sort_rows_t<1>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 2: return radix_sort_rows_t<2>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 3: return radix_sort_rows_t<3>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 4: return radix_sort_rows_t<4>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 5: return radix_sort_rows_t<5>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 6: return radix_sort_rows_t<6>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 7: return radix_sort_rows_t<7>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 8: return radix_sort_rows_t<8>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
+    case 9: return radix_sort_rows_t<9>(keys, vals, keys_alt, vals_alt, m, temp, s, data_passes);
     default: throw std::runtime_error("radix_sort_rows: unsupported row width");
   }
 }

@@ -37,12 +37,14 @@ size_t sort_temp_bytes(int R, u32 m);
 // Exclusive prefix sum of in[0..n) into out; *total_dev receives the sum.
 void launch_scan(const u32* in, u32* out, u32 n, u32* total_dev, void* temp, cudaStream_t s);
 
-// Stable LSD radix sort of m rows of R words (word 0 most significant) with
-// a u32 payload.  Result lands in (keys, vals); (keys_alt, vals_alt) are
-// scratch of the same size.  Digits constant over all rows are skipped.
-// Returns the number of kernels launched.
+// Stable sort of m rows of R words (word 0 most significant) with a u32
+// payload.  Result lands in (keys, vals); (keys_alt, vals_alt) are scratch of
+// the same size.  Up to 2^20 rows: 2048-row chunks sorted in shared memory,
+// then pairwise merges; beyond: LSD radix passes over 8-bit digits, digits
+// constant over all rows skipped.  Returns the number of kernels launched;
+// *data_passes (optional) = full read+write passes over the rows.
 int radix_sort_rows(int R, u64* keys, u32* vals, u64* keys_alt, u32* vals_alt, u32 m, void* temp,
-                     cudaStream_t s);
+                     cudaStream_t s, int* data_passes = nullptr);
 
 // flags[i] = 1 if row i differs from row i-1 (rows sorted).
 void launch_unique_flags(int W, const u64* rows, u32 m, u32* flags, cudaStream_t s);
