@@ -292,6 +292,27 @@ class Engine {
     launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
     launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
     count_launch(3);
+    if (dominance && !self_check && !visited_subsets) {
+      // duplicates only: a child is dropped when it equals its predecessor in
+      // the sorted layer or a visited set — one flag pass, one compaction
+      if (X.vis_count) {
+        timed(3, (double)Nc * 8.0 * W, [&] {
+          launch_clear_members(W, X.vis.as<u64>(), X.vis_count, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(),
+                               stream, X.keymap);
+        });
+        count_launch();
+      }
+      X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(Nc, 1));
+      new_vals.reserve(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
+      const u32 f = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc,
+                            X.rows_alt.as<u64>(), new_vals.as<u32>());
+      if (m) X.unique_growth = (double)f / m;
+      if (verbose)
+        std::fprintf(stderr, "[sw] %s parents=%u children=%u kept=%u (duplicates only) | %.3f ms\n",
+                     forward ? "BFS " : "IBFS", m, Nc, f, vclock() - t_step0);
+      finish_layer(X, W, n, m, f);
+      return;
+    }
     const u32 u = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
                           uq_vals.as<u32>());
     if (m) X.unique_growth = (double)u / m;  // branching before dominance pruning
@@ -357,6 +378,12 @@ class Engine {
     new_vals.reserve(sizeof(u32) * (size_t)std::max<u32>(u, 1));
     const u32 f = compact(W, uq_rows.as<u64>(), uq_vals.as<u32>(), keep.as<u32>(), u, X.rows_alt.as<u64>(),
                           new_vals.as<u32>());
+    finish_layer(X, W, n, m, f);
+  }
+
+  // The kept children (X.rows_alt, origins in new_vals, f of them) become the
+  // new layer of X: recorded for word tracing and merged into the visited list.
+  void finish_layer(Side& X, int W, int n, u32 m, u32 f) {
     std::swap(X.rows.p, X.rows_alt.p);
     std::swap(X.rows.cap, X.rows_alt.cap);
     X.count = f;

@@ -299,6 +299,7 @@ namespace {
 constexpr int kRsThreads = 256;
 constexpr int kRsRounds = 8;
 constexpr u32 kRsTile = kRsThreads * kRsRounds;
+constexpr int kSmallThreads = 1024;  // shared-memory sorts: 2 ranking rounds for 2048 rows
 constexpr u32 kMergeSortMax = 1u << 20;  // up to here: chunk sorts + merge passes; above: radix passes
 
 template <int R>
@@ -425,8 +426,61 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(const u64* __restri
 }
 
 // Whole sort in one block, rows in shared memory (m <= small_sort_max<R>()).
+// block_round_rank for a block of kWarps warps (digit owners: threads < 256).
+template <int kWarps>
+__device__ __forceinline__ u32 block_round_rank_n(u32 d, u32* s_base, u32 (*s_wcnt)[256]) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32 peers = __match_any_sync(kFull, d);
+  const u32 lrank = __popc(peers & lanemask_lt());
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s_wcnt[warp][lane * 8 + j] = 0;
+  __syncwarp();
+  if (d < 256 && lrank == 0) s_wcnt[warp][d] = __popc(peers);
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    const int t = threadIdx.x;  // digit owned by this thread
+    u32 run = s_base[t];
+#pragma unroll 8
+    for (int w = 0; w < kWarps; ++w) {
+      u32 c = s_wcnt[w][t];
+      s_wcnt[w][t] = run;
+      run += c;
+    }
+    s_base[t] = run;
+  }
+  __syncthreads();
+  u32 r = (d < 256) ? s_wcnt[warp][d] + lrank : 0;
+  __syncthreads();
+  return r;
+}
+
+// Exclusive prefix sum of h[0..256) in place by the first 256 threads (warp
+// scans, then the 8 warp totals); tmp: 8 words of scratch.  Ends with a
+// block barrier.
+__device__ __forceinline__ void block_exclusive_scan_256(u32* h, u32* tmp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  u32 v = 0, x = 0;
+  if (threadIdx.x < 256) {
+    v = h[threadIdx.x];
+    x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 y = __shfl_up_sync(kFull, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) tmp[warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 256) {
+    u32 before = 0;
+    for (int w = 0; w < warp; ++w) before += tmp[w];
+    h[threadIdx.x] = before + x - v;
+  }
+  __syncthreads();
+}
+
 template <int R>
-__global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u32 m_total, u32 chunk) {
+__global__ void __launch_bounds__(kSmallThreads) k_rs_small(u64* keys, u32* vals, u32 m_total, u32 chunk) {
   // block b sorts rows [b * chunk, min(m_total, (b + 1) * chunk))
   const u32 base = blockIdx.x * chunk;
   const u32 m = min(chunk, m_total - base);
@@ -439,7 +493,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u
   u32* vb = va + m;
   __shared__ u32 s_hist[256];
   __shared__ u32 s_base[256];
-  __shared__ u32 s_wcnt[8][256];
+  __shared__ u32 s_wcnt[kSmallThreads / 32][256];
   __shared__ u64 s_or[R], s_and[R];
   if (threadIdx.x < R) {
     s_or[threadIdx.x] = 0;
@@ -453,7 +507,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u
       o[w] = 0;
       a[w] = ~0ULL;
     }
-    for (u32 i = threadIdx.x; i < m; i += kRsThreads) {
+    for (u32 i = threadIdx.x; i < m; i += kSmallThreads) {
 #pragma unroll
       for (int w = 0; w < R; ++w) {
         u64 v = keys[(size_t)i * R + w];
@@ -470,30 +524,24 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u
     }
   }
   __syncthreads();
-  const u32 rounds = (m + kRsThreads - 1) / kRsThreads;
+  const u32 rounds = (m + kSmallThreads - 1) / kSmallThreads;
   for (int word = R - 1; word >= 0; --word) {
     const u64 vary = s_or[word] ^ s_and[word];
     for (int shift = 0; shift < 64; shift += 8) {
       if (((vary >> shift) & 255ULL) == 0) continue;
-      s_hist[threadIdx.x] = 0;
-      s_base[threadIdx.x] = 0;
-      __syncthreads();
-      for (u32 i = threadIdx.x; i < m; i += kRsThreads)
-        atomicAdd(&s_hist[(ka[(size_t)i * R + word] >> shift) & 255ULL], 1u);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        u32 run = 0;
-        for (int d = 0; d < 256; ++d) {
-          u32 c = s_hist[d];
-          s_hist[d] = run;
-          run += c;
-        }
+      if (threadIdx.x < 256) {
+        s_hist[threadIdx.x] = 0;
+        s_base[threadIdx.x] = 0;
       }
       __syncthreads();
+      for (u32 i = threadIdx.x; i < m; i += kSmallThreads)
+        atomicAdd(&s_hist[(ka[(size_t)i * R + word] >> shift) & 255ULL], 1u);
+      __syncthreads();
+      block_exclusive_scan_256(s_hist, s_wcnt[0]);
       for (u32 r = 0; r < rounds; ++r) {
-        u32 i = r * kRsThreads + threadIdx.x;
+        u32 i = r * kSmallThreads + threadIdx.x;
         u32 d = i < m ? (u32)((ka[(size_t)i * R + word] >> shift) & 255ULL) : 256u;
-        u32 rank = block_round_rank(d, s_base, s_wcnt);
+        u32 rank = block_round_rank_n<kSmallThreads / 32>(d, s_base, s_wcnt);
         if (d < 256) {
           u32 dst = s_hist[d] + rank;
 #pragma unroll
@@ -510,7 +558,7 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_small(u64* keys, u32* vals, u
       vb = tv;
     }
   }
-  for (u32 i = threadIdx.x; i < m; i += kRsThreads) {
+  for (u32 i = threadIdx.x; i < m; i += kSmallThreads) {
 #pragma unroll
     for (int w = 0; w < R; ++w) keys[(size_t)i * R + w] = ka[(size_t)i * R + w];
     vals[i] = va[i];
@@ -574,7 +622,7 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
       const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
       SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
     });
-    k_rs_small<R><<<1, kRsThreads, smem, s>>>(keys, vals, m, m);
+    k_rs_small<R><<<1, kSmallThreads, smem, s>>>(keys, vals, m, m);
     SW_LAUNCH_CHECK();
     if (data_passes) *data_passes = 1;
     return 1;
@@ -591,7 +639,7 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
       SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
     });
     const size_t smem = (size_t)chunk * (2 * R * sizeof(u64) + 2 * sizeof(u32));
-    k_rs_small<R><<<nchunks, kRsThreads, smem, s>>>(keys, vals, m, chunk);
+    k_rs_small<R><<<nchunks, kSmallThreads, smem, s>>>(keys, vals, m, chunk);
     SW_LAUNCH_CHECK();
     u64 *ki = keys, *ko = keys_alt;
     u32 *vi = vals, *vo = vals_alt;
@@ -926,6 +974,42 @@ __global__ void k_member_key(const u64* __restrict__ V, u32 nv, const u64* __res
       return;
     }
   }
+}
+
+// flags[i] = 0 for rows of C (with flags[i] = 1) equal to some row of V.
+template <int W>
+__global__ void k_clear_members(const u64* __restrict__ V, u32 nv, const u64* __restrict__ C, u32 nc, KeyMap map,
+                                u32* __restrict__ flags) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nc || !flags[i]) return;
+  const u64* x = C + (size_t)i * W;
+  u64 x0, x1;
+  layer_key<W>(x, map, x0, x1);
+  u32 lo = 0, hi = nv;
+  while (lo < hi) {
+    const u32 mid = (lo + hi) >> 1;
+    u64 y0, y1;
+    layer_key<W>(V + (size_t)mid * W, map, y0, y1);
+    if (y0 < x0 || (y0 == x0 && y1 < x1)) lo = mid + 1;
+    else hi = mid;
+  }
+  for (u32 j = lo; j < nv; ++j) {
+    const u64* y = V + (size_t)j * W;
+    u64 y0, y1;
+    layer_key<W>(y, map, y0, y1);
+    if (y0 != x0 || y1 != x1) break;
+    if (row_eq<W>(x, y)) {
+      flags[i] = 0u;
+      return;
+    }
+  }
+}
+
+void launch_clear_members(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
+                          const KeyMap& map) {
+  if (!nc || !nv) return;
+  SW_DISPATCH_W(W, (k_clear_members<WW><<<(nc + 255) / 256, 256, 0, s>>>(V, nv, C, nc, map, flags)));
+  SW_LAUNCH_CHECK();
 }
 
 void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,

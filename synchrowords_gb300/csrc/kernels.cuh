@@ -101,6 +101,10 @@ void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* ou
 // V and C sorted by the same layer key.
 void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
                        const KeyMap& map = KeyMap{});
+// flags[i] = 0 where flags[i] = 1 and row i of C equals a row of V (same
+// layer-key order as launch_member_key).
+void launch_clear_members(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
+                          const KeyMap& map = KeyMap{});
 // counts[q] += rows containing state q (counts: 64*W entries, caller-zeroed).
 void launch_state_counts(int W, const u64* rows, u32 m, u32* counts, cudaStream_t s);
 
