@@ -300,12 +300,14 @@ constexpr int kRsThreads = 256;
 constexpr int kRsRounds = 8;
 constexpr u32 kRsTile = kRsThreads * kRsRounds;
 constexpr int kSmallThreads = 1024;  // shared-memory sorts: 2 ranking rounds for 2048 rows
+constexpr int kSmallRounds = 2;      // rows per thread in a shared-memory sort
 constexpr u32 kMergeSortMax = 1u << 20;  // up to here: chunk sorts + merge passes; above: radix passes
 
 template <int R>
 constexpr u32 small_sort_max() {
   return R <= 4 ? 2048u : 1024u;
 }
+static_assert(2048u <= (u32)kSmallThreads * kSmallRounds, "a shared-memory sort holds its rows in kSmallRounds rounds");
 
 // Per-round stable ranking inside a 256-thread block.  `d` is this thread's
 // digit (256 = no item).  s_base[256] carries counts of earlier rounds,
@@ -529,21 +531,30 @@ __global__ void __launch_bounds__(kSmallThreads) k_rs_small(u64* keys, u32* vals
     const u64 vary = s_or[word] ^ s_and[word];
     for (int shift = 0; shift < 64; shift += 8) {
       if (((vary >> shift) & 255ULL) == 0) continue;
-      if (threadIdx.x < 256) {
-        s_hist[threadIdx.x] = 0;
-        s_base[threadIdx.x] = 0;
-      }
+      // rank every item among equal digits first (the running per-digit
+      // counts end as the digit histogram), then scan the histogram and
+      // scatter: no separate counting pass
+      if (threadIdx.x < 256) s_base[threadIdx.x] = 0;
       __syncthreads();
-      for (u32 i = threadIdx.x; i < m; i += kSmallThreads)
-        atomicAdd(&s_hist[(ka[(size_t)i * R + word] >> shift) & 255ULL], 1u);
+      u32 dr[kSmallRounds], rk[kSmallRounds];
+#pragma unroll
+      for (u32 r = 0; r < (u32)kSmallRounds; ++r) {
+        dr[r] = 256u;
+        rk[r] = 0;
+        if (r < rounds) {
+          const u32 i = r * kSmallThreads + threadIdx.x;
+          dr[r] = i < m ? (u32)((ka[(size_t)i * R + word] >> shift) & 255ULL) : 256u;
+          rk[r] = block_round_rank_n<kSmallThreads / 32>(dr[r], s_base, s_wcnt);
+        }
+      }
+      if (threadIdx.x < 256) s_hist[threadIdx.x] = s_base[threadIdx.x];
       __syncthreads();
       block_exclusive_scan_256(s_hist, s_wcnt[0]);
-      for (u32 r = 0; r < rounds; ++r) {
-        u32 i = r * kSmallThreads + threadIdx.x;
-        u32 d = i < m ? (u32)((ka[(size_t)i * R + word] >> shift) & 255ULL) : 256u;
-        u32 rank = block_round_rank_n<kSmallThreads / 32>(d, s_base, s_wcnt);
-        if (d < 256) {
-          u32 dst = s_hist[d] + rank;
+#pragma unroll
+      for (u32 r = 0; r < (u32)kSmallRounds; ++r) {
+        if (dr[r] < 256) {
+          const u32 i = r * kSmallThreads + threadIdx.x;
+          const u32 dst = s_hist[dr[r]] + rk[r];
 #pragma unroll
           for (int w = 0; w < R; ++w) kb[(size_t)dst * R + w] = ka[(size_t)i * R + w];
           vb[dst] = va[i];
