@@ -21,8 +21,13 @@ for _name, _size in (("phi", FEAT * EMB), ("c", EMB), ("w1", EMB * HID), ("b1", 
 PARAMS = _o
 
 
+EXACT = False  # True: no bf16 rounding, float64 throughout (for finite-difference checks)
+
+
 def bf16(x) -> np.ndarray:
     """Round float32 to bf16 (nearest even), returned as float32."""
+    if EXACT:
+        return np.asarray(x, dtype=np.float64)
     u = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32).astype(np.uint64)
     u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
     return u.astype(np.uint32).view(np.float32)
@@ -31,7 +36,8 @@ def bf16(x) -> np.ndarray:
 def unpack(p: np.ndarray) -> dict:
     shapes = {"phi": (FEAT, EMB), "c": (EMB,), "w1": (EMB, HID), "b1": (HID,), "w2": (HID, HID), "b2": (HID,),
               "w3": (HID,), "b3": (1,)}
-    return {k: np.asarray(p[o:o + s], dtype=np.float32).reshape(shapes[k]) for k, (o, s) in OFF.items()}
+    dt = np.float64 if EXACT else np.float32
+    return {k: np.asarray(p[o:o + s], dtype=dt).reshape(shapes[k]) for k, (o, s) in OFF.items()}
 
 
 def bits(sets_ref8: np.ndarray, n: int) -> np.ndarray:
@@ -53,7 +59,7 @@ def forward(p: np.ndarray, feat: np.ndarray, b: np.ndarray):
     h2 = bf16(np.maximum(h2pre, 0))
     y = h2 @ P["w3"] + P["b3"][0]
     cache = dict(P=P, fb=fb, epre=epre, b=b, x=x, h1pre=h1pre, h1=h1, h2pre=h2pre, h2=h2, y=y)
-    return y.astype(np.float32), cache
+    return (y if EXACT else y.astype(np.float32)), cache
 
 
 def backward(cache: dict, t: np.ndarray):
@@ -63,10 +69,10 @@ def backward(cache: dict, t: np.ndarray):
     B = len(y)
     d = y - t
     loss = float(np.mean(d * d))
-    dy = (2.0 * d / B).astype(np.float32)
+    dy = 2.0 * d / B if EXACT else (2.0 * d / B).astype(np.float32)
     g = {}
     g["w3"] = cache["h2"].T @ dy
-    g["b3"] = np.array([dy.sum()], dtype=np.float32)
+    g["b3"] = np.array([dy.sum()])
     dh2 = np.outer(dy, P["w3"]) * (cache["h2pre"] > 0)
     g["b2"] = dh2.sum(0)
     dh2b = bf16(dh2)
@@ -79,7 +85,7 @@ def backward(cache: dict, t: np.ndarray):
     de = (cache["b"].T @ dx) * (cache["epre"] > 0)
     g["c"] = de.sum(0)
     g["phi"] = cache["fb"].T @ bf16(de)
-    flat = np.zeros(PARAMS, dtype=np.float32)
+    flat = np.zeros(PARAMS, dtype=np.float64 if EXACT else np.float32)
     for k, (o, s) in OFF.items():
-        flat[o:o + s] = np.asarray(g[k], dtype=np.float32).reshape(-1)
+        flat[o:o + s] = np.asarray(g[k]).reshape(-1)
     return flat, loss

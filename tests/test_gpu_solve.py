@@ -98,6 +98,25 @@ def test_random_wide_rows_exact(ctx, n, seed):
     check_word(d, n, 2, r)
 
 
+def cored_dfa(n, core, k, seed):
+    """A random `core`-state automaton plus n - core transient states that map
+    straight into the core: eight-word rows with a search the oracle finishes
+    at once."""
+    from synchrowords_gb300.generate import splitmix64
+    g = splitmix64(seed)
+    return list(random_dfa(core, k, seed)) + [next(g) % core for _ in range((n - core) * k)]
+
+
+@pytest.mark.parametrize("n,core,k,seed", [(449, 60, 2, 7), (470, 60, 2, 8), (512, 80, 3, 9), (300, 100, 2, 10)])
+def test_wide_rows_with_transient_states(ctx, n, core, k, seed):
+    d = cored_dfa(n, core, k, seed)
+    ref = oracle.exact(d, n, k, oracle.ExactParams(threads=8))
+    for plan in (EXACT, BEAM_EXACT):
+        r = ctx.solve(d, n, k, plan)
+        assert (r.lower, r.upper) == (ref.lower, ref.upper)
+        check_word(d, n, k, r)
+
+
 @pytest.mark.parametrize("seed", [5, 6])
 def test_random_n200_beam_exact(ctx, seed):
     n, k = 200, 2

@@ -162,3 +162,42 @@ def test_oracle_brute_matches_reference_fixture():
         assert (want < 0) == bool(r.get("non_synchro"))
         if want >= 0:
             assert (r["lower"], r["upper"]) == (want, want)
+
+
+def test_mlp_oracle_backward_matches_finite_differences():
+    """The numpy restatement of the distance model (the checker of the GPU
+    gradients) is itself checked: without bf16 rounding, in float64, its
+    backward pass matches central differences of its forward pass."""
+    import numpy as np
+    from oracle import mlp
+    rng = np.random.default_rng(11)
+    n = 23
+    feat = rng.normal(size=(n, mlp.FEAT))
+    bits = (rng.random((40, n)) < 0.4).astype(np.float64)
+    t = rng.normal(10.0, 3.0, size=40)
+    p = rng.normal(0, 0.2, size=mlp.PARAMS)
+    mlp.EXACT = True
+    try:
+        _, cache = mlp.forward(p, feat, bits)
+        g, _ = mlp.backward(cache, t)
+
+        def loss(q):
+            y, _ = mlp.forward(q, feat, bits)
+            return float(np.mean((y - t) ** 2))
+
+        idx = list(rng.choice(mlp.PARAMS, 60, replace=False)) + [mlp.OFF["b3"][0], mlp.OFF["c"][0] + 3]
+        for i in idx:
+            e = np.zeros(mlp.PARAMS)
+            e[i] = 1e-5
+            num = (loss(p + e) - loss(p - e)) / 2e-5
+            assert abs(num - g[i]) <= 1e-5 + 1e-4 * abs(num), (i, num, g[i])
+    finally:
+        mlp.EXACT = False
+
+
+def test_bf16_rounding_is_nearest_even():
+    import numpy as np
+    from oracle import mlp
+    x = np.array([1.0, 1.0 + 2 ** -8, 1.0 + 3 * 2 ** -8, 1.0 + 2 ** -7 + 2 ** -9, -2.5e-3], dtype=np.float32)
+    # ties go to the even mantissa; 7 fraction bits near 1
+    assert mlp.bf16(x).tolist() == [1.0, 1.0, 1.0 + 2 ** -6, 1.0 + 2 ** -7, -0.00250244140625]
