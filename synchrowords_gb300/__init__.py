@@ -12,6 +12,7 @@ is missing, and creating a context fails when no CUDA device is present.
 from __future__ import annotations
 
 import ctypes
+import itertools
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import List, Optional, Sequence, Tuple
@@ -351,23 +352,29 @@ class Context:
         count = len(automata)
         if count == 0:
             return []
-        ns = _u32([a[0] for a in automata])
-        ks = _u32([a[1] for a in automata])
-        deltas = _u32([x for a in automata for x in a[2]])
+        ns = np.fromiter((a[0] for a in automata), dtype=np.uint32, count=count)
+        ks = np.fromiter((a[1] for a in automata), dtype=np.uint32, count=count)
+        total = int(np.dot(ns.astype(np.int64), ks.astype(np.int64)))
+        if any(len(a[2]) != a[0] * a[1] for a in automata):
+            raise ValueError("each automaton needs n * k transitions")
+        deltas = np.fromiter(itertools.chain.from_iterable(a[2] for a in automata), dtype=np.uint32, count=total)
+        # one word buffer for the batch: automaton i gets max(4096, 4 n^2) entries
+        caps = np.maximum(1 << 12, 4 * ns.astype(np.uint64) ** 2)
+        offs = np.zeros(count + 1, dtype=np.uint64)
+        np.cumsum(caps, out=offs[1:])
+        words = np.zeros(int(offs[-1]), dtype=np.uint32)
         res = (_Result * count)()
-        bufs = []
-        for i, (n, k, _) in enumerate(automata):
-            cap = max(1 << 12, 4 * n * n)
-            b = np.zeros(cap, dtype=np.uint32)
-            bufs.append(b)
-            res[i].word = b.ctypes.data_as(_U32P)
-            res[i].word_capacity = cap
+        raw = np.frombuffer(res, dtype=np.uint8).reshape(count, ctypes.sizeof(_Result))
+        o = _Result.word.offset
+        raw[:, o:o + 8] = (np.uint64(words.ctypes.data) + np.uint64(4) * offs[:-1]).view(np.uint8).reshape(count, 8)
+        o = _Result.word_capacity.offset
+        raw[:, o:o + 4] = caps.astype(np.uint32).view(np.uint8).reshape(count, 4)
         _check(self._lib.sw_solve_batch(self._h, count, deltas.ctypes.data_as(_U32P), ns.ctypes.data_as(_U32P),
                                         ks.ctypes.data_as(_U32P), plan_json.encode(), res, workers))
         out = []
         for i in range(count):
             r = res[i]
-            word = bufs[i][: r.word_len].tolist() if r.has_word else None
+            word = words[int(offs[i]): int(offs[i]) + r.word_len].tolist() if r.has_word else None
             runs = [(r.runs[j].name.decode(), r.runs[j].ms) for j in range(r.n_runs)]
             stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
             out.append(Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats))

@@ -1,11 +1,15 @@
 // C ABI (include/synchrowords.h).  Every entry point catches exceptions and
 // turns them into status codes with a thread-local message, where the
 // reference exits or throws across dlopen (app/jit.hpp:61-83).
+#include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <vector>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -13,12 +17,23 @@
 
 #include "../../include/synchrowords.h"
 #include "automaton.hpp"
+#include "algos.cuh"
 #include "exact.hpp"
 #include "plan.hpp"
+
+// Device state of the batched small-automaton launch (batch_small.cu).
+struct SmallBatchState {
+  cudaStream_t stream = nullptr;
+  sw::DevBuf inst, delta, seeds, results, words, origins, visited, counter;
+  ~SmallBatchState() {
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
 
 struct sw_context {
   std::unique_ptr<sw::Solver> solver;
   std::vector<std::unique_ptr<sw::Solver>> workers;  // extra streams for sw_solve_batch
+  SmallBatchState small;
 };
 
 namespace {
@@ -214,47 +229,228 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     workers = std::max<uint32_t>(1, std::min<uint32_t>(workers, count));
     while (ctx->workers.size() + 1 < workers)
       ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
-    if (ctx->solver->has_model()) {  // every worker scores with the context's distance model
+    using clk = std::chrono::steady_clock;
+    const bool verbose = std::getenv("SYNCHRO_BATCH_VERBOSE") != nullptr;
+    const auto h0 = clk::now();
+    auto since = [&](clk::time_point a) { return std::chrono::duration<double, std::milli>(clk::now() - a).count(); };
+    // every worker that runs an instance scores with the context's distance model (copied on first use)
+    bool model_copied = !ctx->solver->has_model();
+    auto copy_model = [&](uint32_t nw) {
+      if (model_copied) return;
       std::vector<float> model(SW_MLP_PARAMS);
       ctx->solver->get_model(model.data());
-      for (uint32_t w = 1; w < workers; ++w) ctx->workers[w - 1]->set_model(model.data());
+      for (uint32_t w = 1; w < nw; ++w) ctx->workers[w - 1]->set_model(model.data());
+      model_copied = true;
+    };
+    // Small automata whose plan is a plain Exact run go to one persistent
+    // batched launch (batch_small.cu); the rest, and any automaton that
+    // launch cannot finish, run on the worker streams.
+    std::vector<uint32_t> streamed, small[4];
+    std::map<std::pair<uint32_t, uint32_t>, sw_plan> plans;
+    std::vector<std::vector<uint32_t>> seeds(count);
+    std::vector<uint32_t> max_len(count, 0);
+    for (uint32_t i = 0; i < count; ++i) {
+      const uint32_t n = ns[i], k = ks[i];
+      bool ok = n >= 2 && n <= 256 && k >= 1 && k <= 4;
+      if (ok) {
+        auto key = std::make_pair(n, k);
+        auto it = plans.find(key);
+        if (it == plans.end()) {
+          sw_plan p;
+          sw::plan_from_json(plan_json, n, k, &p);
+          it = plans.emplace(key, p).first;
+        }
+        const sw_plan& p = it->second;
+        ok = p.n_algorithms == 1 && p.algorithms[0].kind == SW_ALGO_EXACT && p.upper_bound >= 1;
+        if (ok) {
+          // No synchronisation test here: the batched search reports a length
+          // only when its two sides meet, which proves a reset word; an
+          // automaton without one ends over capacity or unfinished and the
+          // streamed path settles it.
+          const sw::Automaton A = sw::make_automaton(deltas + off[i], n, k);
+          seeds[i] = sw::backward_seeds(A);
+          std::sort(seeds[i].begin(), seeds[i].end());
+          ok = !seeds[i].empty();
+          // plain Exact with no word behind the bound searches lengths up to the bound
+          max_len[i] = (uint32_t)std::min<uint64_t>(p.upper_bound, 512);
+        }
+      }
+      if (ok)
+        small[(n - 1) / 64].push_back(i);
+      else
+        streamed.push_back(i);
     }
-    std::atomic<uint32_t> next{0};
+    const double ms_classify = since(h0);
+    SmallBatchState& S = ctx->small;
+    const bool any_small = !small[0].empty() || !small[1].empty() || !small[2].empty() || !small[3].empty();
+    const uint32_t word_stride = 512;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    int small_launches = 0;
+    if (any_small) {
+      SW_CUDA(cudaSetDevice(ctx->solver->device()));
+      if (!S.stream) SW_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+      const uint32_t blocks = (uint32_t)sw::small_batch_blocks();
+      std::vector<sw::SmallInstance> inst;
+      std::vector<uint8_t> dpool, spool;
+      std::vector<uint32_t> order;  // batch slot -> instance
+      size_t class_start[5] = {0, 0, 0, 0, 0};
+      for (int c = 0; c < 4; ++c) {
+        class_start[c] = inst.size();
+        for (uint32_t i : small[c]) {
+          sw::SmallInstance I{ns[i], ks[i], (uint32_t)dpool.size(), (uint32_t)spool.size(),
+                              (uint32_t)seeds[i].size(), max_len[i]};
+          for (size_t e = 0; e < (size_t)ns[i] * ks[i]; ++e) dpool.push_back((uint8_t)deltas[off[i] + e]);
+          for (uint32_t q : seeds[i]) spool.push_back((uint8_t)q);
+          inst.push_back(I);
+          order.push_back(i);
+        }
+      }
+      class_start[4] = inst.size();
+      S.inst.reserve(sizeof(sw::SmallInstance) * inst.size());
+      S.delta.reserve(std::max<size_t>(dpool.size(), 1));
+      S.seeds.reserve(std::max<size_t>(spool.size(), 1));
+      S.results.reserve(sizeof(sw::SmallResult) * inst.size());
+      S.words.reserve((size_t)word_stride * inst.size());
+      size_t ow = 0, vw = 0;
+      for (int c = 0; c < 4; ++c)
+        if (!small[c].empty()) {
+          ow = std::max(ow, sw::small_batch_origin_words(c + 1, blocks));
+          vw = std::max(vw, sw::small_batch_visited_words(c + 1, blocks));
+        }
+      S.origins.reserve(sizeof(uint32_t) * ow);
+      S.visited.reserve(sizeof(uint64_t) * vw);
+      S.counter.reserve(sizeof(uint32_t) * 2);
+      SW_CUDA(cudaMemcpyAsync(S.inst.p, inst.data(), sizeof(sw::SmallInstance) * inst.size(), cudaMemcpyHostToDevice,
+                              S.stream));
+      SW_CUDA(cudaMemcpyAsync(S.delta.p, dpool.data(), dpool.size(), cudaMemcpyHostToDevice, S.stream));
+      SW_CUDA(cudaMemcpyAsync(S.seeds.p, spool.data(), spool.size(), cudaMemcpyHostToDevice, S.stream));
+      SW_CUDA(cudaEventCreate(&t0));
+      SW_CUDA(cudaEventCreate(&t1));
+      SW_CUDA(cudaEventRecord(t0, S.stream));
+      for (int c = 0; c < 4; ++c) {
+        const size_t a = class_start[c], b = class_start[c + 1];
+        if (a == b) continue;
+        ++small_launches;
+        sw::launch_small_batch(c + 1, S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a), S.delta.as<uint8_t>(),
+                               S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
+                               S.words.as<uint8_t>() + a * word_stride, word_stride, S.origins.as<uint32_t>(),
+                               S.visited.as<sw::u64>(), blocks, S.counter.as<uint32_t>(), S.stream);
+      }
+      SW_CUDA(cudaEventRecord(t1, S.stream));
+      // results come back after the streamed instances are done
+      small[0] = order;  // reuse: slot order
+    }
     std::atomic<int> first_rc{SW_OK};
     std::mutex err_mu;
     std::string first_err;
-    auto work = [&](sw::Solver& solver) {
-      uint32_t i;
-      while ((i = next++) < count && first_rc.load() == SW_OK) {
-        int rc;
-        std::string err;
-        try {
-          sw_plan plan;
-          sw::plan_from_json(plan_json, ns[i], ks[i], &plan);
-          rc = run_plan(solver, deltas + off[i], ns[i], ks[i], &plan, &results[i], err);
-        } catch (const sw::CudaError& e) {
-          rc = SW_ERR_CUDA;
-          err = e.what();
-        } catch (const std::invalid_argument& e) {
-          rc = SW_ERR_INVALID_ARGUMENT;
-          err = e.what();
-        } catch (const std::exception& e) {
-          rc = SW_ERR_INTERNAL;
-          err = e.what();
-        }
-        if (rc != SW_OK) {
-          std::lock_guard<std::mutex> g(err_mu);
-          if (first_rc.load() == SW_OK) {
-            first_rc = rc;
-            first_err = "instance " + std::to_string(i) + ": " + err;
+    auto run_pool = [&](const std::vector<uint32_t>& todo) {
+      if (todo.empty()) return;
+      std::atomic<size_t> next{0};
+      auto work = [&](sw::Solver& solver) {
+        size_t t;
+        while ((t = next++) < todo.size() && first_rc.load() == SW_OK) {
+          const uint32_t i = todo[t];
+          int rc;
+          std::string err;
+          try {
+            sw_plan plan;
+            sw::plan_from_json(plan_json, ns[i], ks[i], &plan);
+            rc = run_plan(solver, deltas + off[i], ns[i], ks[i], &plan, &results[i], err);
+          } catch (const sw::CudaError& e) {
+            rc = SW_ERR_CUDA;
+            err = e.what();
+          } catch (const std::invalid_argument& e) {
+            rc = SW_ERR_INVALID_ARGUMENT;
+            err = e.what();
+          } catch (const std::exception& e) {
+            rc = SW_ERR_INTERNAL;
+            err = e.what();
+          }
+          if (rc != SW_OK) {
+            std::lock_guard<std::mutex> g(err_mu);
+            if (first_rc.load() == SW_OK) {
+              first_rc = rc;
+              first_err = "instance " + std::to_string(i) + ": " + err;
+            }
           }
         }
-      }
+      };
+      const uint32_t nw = std::min<uint32_t>(workers, (uint32_t)todo.size());
+      copy_model(workers);
+      std::vector<std::thread> th;
+      for (uint32_t w = 1; w < nw; ++w) th.emplace_back(work, std::ref(*ctx->workers[w - 1]));
+      work(*ctx->solver);
+      for (auto& t : th) t.join();
     };
-    std::vector<std::thread> th;
-    for (uint32_t w = 1; w < workers; ++w) th.emplace_back(work, std::ref(*ctx->workers[w - 1]));
-    work(*ctx->solver);
-    for (auto& t : th) t.join();
+    const double ms_launch = since(h0) - ms_classify;
+    const auto h1 = clk::now();
+    run_pool(streamed);
+    const double ms_streamed = since(h1);
+    if (any_small) {
+      const auto h2 = clk::now();
+      const std::vector<uint32_t>& order = small[0];
+      const size_t m = order.size();
+      std::vector<sw::SmallResult> R(m);
+      std::vector<uint8_t> words((size_t)word_stride * m);
+      SW_CUDA(cudaMemcpyAsync(R.data(), S.results.p, sizeof(sw::SmallResult) * m, cudaMemcpyDeviceToHost, S.stream));
+      SW_CUDA(cudaMemcpyAsync(words.data(), S.words.p, words.size(), cudaMemcpyDeviceToHost, S.stream));
+      SW_CUDA(cudaStreamSynchronize(S.stream));
+      float ms = 0;
+      SW_CUDA(cudaEventElapsedTime(&ms, t0, t1));
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      std::vector<uint32_t> again;
+      bool first = true;
+      const double ms_wait = since(h2);
+      for (size_t t = 0; t < m; ++t) {
+        const uint32_t i = order[t];
+        if (R[t].status != 0) {
+          again.push_back(i);
+          continue;
+        }
+        sw_result* r = &results[i];
+        uint32_t* wb = r->word;
+        const uint32_t cap = r->word_capacity;
+        std::memset(r, 0, sizeof(*r));
+        r->word = wb;
+        r->word_capacity = cap;
+        std::vector<uint32_t> word(words.begin() + t * word_stride, words.begin() + t * word_stride + R[t].word_len);
+        const sw::Automaton A = sw::make_automaton(deltas + off[i], ns[i], ks[i]);
+        if (word.size() != R[t].length || sw::apply_word(A, word).size() != 1)
+          throw std::runtime_error("internal: batched word does not synchronize");
+        r->mlsw_lower_bound = r->mlsw_upper_bound = R[t].length;
+        r->has_word = 1;
+        r->word_len = R[t].length;
+        if (wb) {
+          if (cap < word.size()) return fail(SW_ERR_CAPACITY, "instance " + std::to_string(i) + ": word buffer too small");
+          std::memcpy(wb, word.data(), sizeof(uint32_t) * word.size());
+        }
+        const sw_plan& p = plans.at(std::make_pair(ns[i], ks[i]));
+        std::strncpy(r->runs[0].name, p.algorithms[0].name, SW_NAME_LEN - 1);
+        r->runs[0].ms = 0;
+        r->n_runs = 1;
+        r->stats.device_ms = ms / (double)m;
+        if (first) r->stats.kernel_launches = (uint64_t)small_launches;  // the batch's launches, counted once
+        first = false;
+      }
+      const double ms_results = since(h2) - ms_wait;
+      if (verbose) {
+        size_t st[3] = {0, 0, 0};
+        std::map<std::pair<uint32_t, uint32_t>, size_t> over;  // (capacity, set width) -> automata
+        for (size_t t = 0; t < m; ++t) {
+          st[std::min<uint32_t>(R[t].status, 2)]++;
+          if (R[t].status == 1) over[{R[t].why & 255u, (ns[order[t]] + 63) / 64}]++;
+        }
+        for (const auto& kv : over)
+          std::fprintf(stderr, "[sw] batched launch: capacity %u (W=%u): %zu automata\n", kv.first.first,
+                       kv.first.second, kv.second);
+        std::fprintf(stderr,
+                     "[sw] batched launch: %zu automata, %zu solved, %zu over capacity, %zu unfinished, %.3f ms on "
+                     "the device; host: classify %.3f, upload+launch %.3f, streamed %.3f, wait %.3f, results %.3f ms\n",
+                     m, st[0], st[1], st[2], (double)ms, ms_classify, ms_launch, ms_streamed, ms_wait, ms_results);
+      }
+      run_pool(again);
+    }
     if (first_rc.load() != SW_OK) return fail(first_rc.load(), first_err);
     return SW_OK;
   });

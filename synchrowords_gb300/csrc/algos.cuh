@@ -45,4 +45,31 @@ void launch_brute_level(const uint16_t* delta, int n, int k, const u32* frontier
 void launch_brute_parent(const uint16_t* delta, int n, int k, const u32* level, u32 count, u32 target, u64* best,
                          cudaStream_t s);
 
+// ---- Batched exact search for small automata (batch_small.cu) -----------
+
+// One automaton of a batch: n <= 64 W states, k <= 4 letters; delta[q*k + a]
+// (u8) at delta_off of the delta pool, its backward seeds (ascending) at
+// seed_off of the seed pool; lengths 1..max_len are searched.
+struct SmallInstance {
+  u32 n, k, delta_off, seed_off, seed_count, max_len;
+};
+// status 0: found, length and word_len letters at words + i * word_stride;
+// 1: lists outgrew the shared-memory capacities (solve it another way);
+// 2: no meeting pair within max_len.
+// status: 0 solved, 1 over a capacity, 2 no meeting within max_len.
+// why (status 1): bits 0-7 the capacity (1 children, 2 layer, 3 visited,
+// 4 depth, 5 word buffer), bits 8+ the layers searched when it stopped.
+struct SmallResult {
+  u32 status, length, word_len, why;
+};
+
+int small_batch_blocks();
+size_t small_batch_origin_words(int W, u32 blocks);
+size_t small_batch_visited_words(int W, u32 blocks);
+// One persistent launch of `blocks` blocks over `count` automata of set width
+// W (1 to 4 words, n <= 64 W); origins, visited and counter are scratch.
+void launch_small_batch(int W, const SmallInstance* inst, u32 count, const uint8_t* delta_pool,
+                        const uint8_t* seed_pool, SmallResult* results, uint8_t* words, u32 word_stride, u32* origins,
+                        u64* visited, u32 blocks, u32* counter, cudaStream_t s);
+
 }  // namespace sw

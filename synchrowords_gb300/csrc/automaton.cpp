@@ -101,34 +101,42 @@ Automaton permute(const Automaton& A, const std::vector<uint32_t>& order) {
 
 bool is_synchronizing(const Automaton& A) {
   // Backward BFS in the pair graph from the diagonal: every pair must reach it.
-  const uint32_t n = A.n;
+  const uint32_t n = A.n, k = A.k;
   if (n <= 1) return true;
-  std::vector<std::vector<uint32_t>> pre((size_t)n * A.k);
+  // preimages of (state, letter) as one flat list
+  std::vector<uint32_t> start((size_t)n * k + 1, 0), pre((size_t)n * k);
   for (uint32_t q = 0; q < n; ++q)
-    for (uint32_t a = 0; a < A.k; ++a) pre[(size_t)A.at(q, a) * A.k + a].push_back(q);
-  auto id = [n](uint32_t p, uint32_t q) { return (size_t)std::min(p, q) * n + std::max(p, q); };
-  std::vector<char> seen((size_t)n * n, 0);
-  std::deque<std::pair<uint32_t, uint32_t>> dq;
-  for (uint32_t q = 0; q < n; ++q) {
-    seen[id(q, q)] = 1;
-    dq.push_back({q, q});
+    for (uint32_t a = 0; a < k; ++a) start[(size_t)A.at(q, a) * k + a + 1]++;
+  for (size_t i = 0; i < (size_t)n * k; ++i) start[i + 1] += start[i];
+  {
+    std::vector<uint32_t> pos(start.begin(), start.end() - 1);
+    for (uint32_t q = 0; q < n; ++q)
+      for (uint32_t a = 0; a < k; ++a) pre[pos[(size_t)A.at(q, a) * k + a]++] = q;
   }
-  size_t reached = n;
-  while (!dq.empty()) {
-    auto [p, q] = dq.front();
-    dq.pop_front();
-    for (uint32_t a = 0; a < A.k; ++a)
-      for (uint32_t x : pre[(size_t)p * A.k + a])
-        for (uint32_t y : pre[(size_t)q * A.k + a]) {
-          size_t i = id(x, y);
-          if (!seen[i]) {
-            seen[i] = 1;
-            ++reached;
-            dq.push_back({x, y});
+  // unordered pair {p, q}, p <= q, as p * n + q
+  std::vector<char> seen((size_t)n * n, 0);
+  std::vector<uint32_t> queue;
+  queue.reserve((size_t)n * (n + 1) / 2);
+  for (uint32_t q = 0; q < n; ++q) {
+    seen[(size_t)q * n + q] = 1;
+    queue.push_back(q * n + q);
+  }
+  for (size_t h = 0; h < queue.size(); ++h) {
+    const uint32_t p = queue[h] / n, q = queue[h] % n;
+    for (uint32_t a = 0; a < k; ++a) {
+      const size_t pa = (size_t)p * k + a, qa = (size_t)q * k + a;
+      for (uint32_t i = start[pa]; i < start[pa + 1]; ++i)
+        for (uint32_t j = start[qa]; j < start[qa + 1]; ++j) {
+          const uint32_t x = pre[i], y = pre[j];
+          const uint32_t id = x <= y ? x * n + y : y * n + x;
+          if (!seen[id]) {
+            seen[id] = 1;
+            queue.push_back(id);
           }
         }
+    }
   }
-  return reached == (size_t)n * (n + 1) / 2;
+  return queue.size() == (size_t)n * (n + 1) / 2;
 }
 
 HostTables build_tables(const Automaton& A) {
