@@ -59,7 +59,7 @@ WORKLOADS = {
     "n200": (200, 2, 16, PLAN_EXACT, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
     "n48": (48, 2, 64, PLAN_EXACT, "plain exact, 64 random binary DFAs, n=48 (64-bit sets)"),
     "batch4096": (0, 0, 4096, PLAN_EXACT,
-                  "plain exact, 4096 random DFAs, n ~ U[32,160], k ~ U{2,3} (64/128/256-bit sets)"),
+                  "plain exact, 4096 random DFAs, n ~ U[32,160], k ~ U{2,3} (64/128/192-bit sets)"),
     "n320": (320, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=320"),
     "n384": (384, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=384"),
     "n384_learned": (384, 2, 8, PLAN_LEARNED_EXACT,

@@ -311,9 +311,9 @@ int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32
  * loads the library keeps it until the process exits).  Larger set lists are
  * rejected with SW_ERR_CAPACITY.
  *
- * Rows use the device layout: W = 1, 2 or 4 uint64 words for n <= 64, 128,
- * 256, else W = ceil(n / 64) (5 to 8); state q is bit (63 - q % 64) of word
- * q / 64; unused bits are 0; both row arrays start 16-byte aligned.
+ * Rows use the device layout: W = ceil(n / 64) uint64 words (1 to 8); state
+ * q is bit (63 - q % 64) of word q / 64; unused bits are 0; both row arrays
+ * start 16-byte aligned.
  * d_results[i] (uint32) becomes 1 if some d_sets row ⊆ d_checks row i
  * (⊊ when proper), else 0.  The work is queued on `stream` (NULL = default
  * stream); the call returns without waiting for it.  The first call on a

@@ -1,8 +1,8 @@
 // Shared definitions for the synchrowords GB300 library (host + device).
 //
 // Set layout on the device ("MSB-first rows"): a set of n states is a row of
-// W 64-bit words (W = 1, 2 or 4 up to 256 states, else ceil(n/64) = 5..8,
-// so n = 320 / 384 use 40 / 48-byte rows, not 64); state q is
+// W = ceil(n/64) 64-bit words, 1..8 (n = 160 / 320 / 384 use 24 / 40 /
+// 48-byte rows); state q is
 // bit (63 - q % 64) of word q / 64.  With this layout the numeric order of
 // rows (word 0 most significant) is the reference's lexicographic order of
 // sets (state 0 most significant, synchrolib/data_structures/subset.hpp:71-77),
@@ -39,10 +39,7 @@ struct CudaError : std::runtime_error {
 constexpr int kMaxStates = 512;
 constexpr int kMaxLetters = 16;
 
-inline int words_for(int n) {
-  int w = (n + 63) / 64;
-  return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : w;
-}
+inline int words_for(int n) { return n <= 64 ? 1 : (n + 63) / 64; }
 
 // Device-side bit helpers for the MSB-first layout.
 __host__ __device__ inline u64 state_bit(int q) { return 1ULL << (63 - (q & 63)); }

@@ -136,6 +136,7 @@ void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t
   switch (W) {
     SW_EXP(1)
     SW_EXP(2)
+    SW_EXP(3)
     SW_EXP(4)
     SW_EXP(5)
     SW_EXP(6)
@@ -779,6 +780,7 @@ __global__ void k_fill_u32(u32* p, u32 v, u32 m) {
   switch (W) {                                              \
     case 1: { constexpr int WW = 1; __VA_ARGS__; } break;   \
     case 2: { constexpr int WW = 2; __VA_ARGS__; } break;   \
+    case 3: { constexpr int WW = 3; __VA_ARGS__; } break;   \
     case 4: { constexpr int WW = 4; __VA_ARGS__; } break;   \
     case 5: { constexpr int WW = 5; __VA_ARGS__; } break;   \
     case 6: { constexpr int WW = 6; __VA_ARGS__; } break;   \

@@ -197,6 +197,7 @@ void launch_tile_and(int W, const u64* S, u32 m, u64* masks, cudaStream_t s) {
   switch (W) {
     case 1: k_range_and<1><<<blocks, 256, 0, s>>>(S, m, masks); break;
     case 2: k_range_and<2><<<blocks, 256, 0, s>>>(S, m, masks); break;
+    case 3: k_range_and<3><<<blocks, 256, 0, s>>>(S, m, masks); break;
     case 4: k_range_and<4><<<blocks, 256, 0, s>>>(S, m, masks); break;
     case 5: k_range_and<5><<<blocks, 256, 0, s>>>(S, m, masks); break;
     case 6: k_range_and<6><<<blocks, 256, 0, s>>>(S, m, masks); break;
@@ -238,6 +239,7 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
   switch (W) {
     SW_SC(1)
     SW_SC(2)
+    SW_SC(3)
     SW_SC(4)
     SW_SC(5)
     SW_SC(6)

@@ -1,5 +1,5 @@
-"""Uneven batch (BASELINE configs[3] shape): 4096 random automata, n ~ U[32,160],
-k ~ U{2,3}, solved concurrently through sw_solve_batch; every length equals the
+"""Uneven batch of 4096 random automata, n ~ U[32,160], k ~ U{2,3}, solved
+through sw_solve_batch (batched launch plus worker streams); every length equals the
 committed golden (oracle, spot-checked against the compiled reference) and every
 word is verified."""
 import json

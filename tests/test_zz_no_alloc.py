@@ -19,9 +19,8 @@ pytestmark = pytest.mark.gpu
 
 
 def device_rows(sets, n):
-    """Rows in the device layout: W = 1, 2, 4, then ceil(n/64) words, state q at bit 63 - q % 64 of word q / 64."""
-    w = (n + 63) // 64
-    W = 1 if w <= 1 else 2 if w <= 2 else 4 if w <= 4 else w
+    """Rows in the device layout: W = ceil(n/64) words, state q at bit 63 - q % 64 of word q / 64."""
+    W = max(1, (n + 63) // 64)
     out = np.zeros((len(sets), W), dtype=np.uint64)
     for i, s in enumerate(sets):
         for q in s:
@@ -60,6 +59,11 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx, native_lib):
     S3 = random_sets(rng, n3, 1001, 0.08)
     C3 = random_sets(rng, n3, 800, 0.8) + S3[:20]
     cases.append((n3, S3, C3, False))
+    # fourth: 150 states (three-word rows, 24 bytes: tiles of 64 rows stay 16-byte aligned)
+    n4 = 150
+    S4 = random_sets(rng, n4, 1500, 0.1)
+    C4 = random_sets(rng, n4, 700, 0.75) + S4[:25]
+    cases.append((n4, S4, C4, True))
     for n, S, C, proper in cases:
         want = ctx.subsets_check(n, to_rows(S, n), to_rows(C, n), proper=proper).tolist()
         got = run_noalloc(native_lib, n, S, C, proper)
