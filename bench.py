@@ -234,10 +234,15 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
+    tuned = None
+    if args.autotune:
+        tuned = ctx.autotune_batch(dfas, plan)  # untimed; keeps the fastest tuning on ctx
+    step_workers = 0 if args.autotune else args.streams
+
     def one_step():
         launches = 0
         lengths = []
-        for r in ctx.solve_batch(dfas, plan, workers=args.streams):
+        for r in ctx.solve_batch(dfas, plan, workers=step_workers):
             launches += r.stats["kernel_launches"]
             if r.non_synchro:
                 lengths.append(None)  # no reset word exists (uneven batch has a few)
@@ -320,7 +325,8 @@ def run_ours(args, world, rank, local):
         "ms_per_step": round(dev_total / args.steps, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": plan_name(plan),
-                   "streams": args.streams,
+                   "streams": args.streams if not args.autotune else ctx.get_batch_tuning()["workers"],
+                   "batch_tuning": dict(ctx.get_batch_tuning(), autotune_ms=tuned["ms"] if tuned else None),
                    "l2": "flushed (256 MB write) before every timed step", "per_gpu_ms_per_dfa": round(value, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roofline,
@@ -348,6 +354,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="before the warm-up, tune the batch's worker count and batched-launch limit on the workload")
     ap.add_argument("--instances", type=int, default=0,
                     help="solve only the first N DFAs of the workload (profiling runs; 0 = all)")
     args = ap.parse_args()

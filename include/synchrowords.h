@@ -204,9 +204,38 @@ int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k
  * words).  `workers` device streams (0 = min(count, 16)), each driven by its
  * own host thread, solve instances concurrently on the context's GPU.  The
  * reference solves the automata of a file one after another
- * (app/main.cpp:48-78); there is no batched counterpart. */
+ * (app/main.cpp:48-78); there is no batched counterpart.
+ *
+ * Automata of at most 256 states whose plan is a single Exact run and whose
+ * n * log2(k) is at most the context's batched_limit (default 104: binary
+ * automata up to 104 states, ternary up to 65) are first solved by one
+ * persistent batched launch per set width (one GPU block per automaton at a
+ * time); those it cannot finish within its capacities, and every other
+ * automaton, run on the worker streams.  workers = 0 uses the context's
+ * tuned count (sw_autotune_batch / sw_set_batch_tuning), else
+ * min(count, 16). */
 int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
                    const char* plan_json, sw_result* results, uint32_t workers);
+
+typedef struct {
+  uint32_t workers;      /* worker streams when sw_solve_batch gets 0; 0 = min(count, 16) */
+  double batched_limit;  /* n * log2(k) bound for the batched launch; < 0 disables it */
+} sw_batch_tuning;
+
+int sw_get_batch_tuning(sw_context* ctx, sw_batch_tuning* out);
+int sw_set_batch_tuning(sw_context* ctx, const sw_batch_tuning* in);
+
+/* Batch autotuner: times the batch (wall clock, best of `reps` runs, 0 = 1)
+ * first at each candidate worker count with the current batched_limit, then
+ * at each candidate batched_limit with the best worker count, and keeps the
+ * fastest pair as the context's tuning.  NULL candidate lists use the
+ * defaults (workers 8, 12, 16, 24 clipped to count; limits -1, 104, 1024).
+ * ms (if not NULL) receives n_workers + n_limits times in that order (4 + 3
+ * for the defaults); *best the chosen tuning.  results hold the last run. */
+int sw_autotune_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                      const char* plan_json, sw_result* results, const uint32_t* worker_candidates,
+                      uint32_t n_workers, const double* limit_candidates, uint32_t n_limits, uint32_t reps,
+                      double* ms, sw_batch_tuning* best);
 
 /* ---- measurement --------------------------------------------------------
  * No counterpart in the reference (its timers are host RAII timers,

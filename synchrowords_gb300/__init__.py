@@ -99,6 +99,10 @@ class _Result(ctypes.Structure):
                 ("n_runs", ctypes.c_uint32), ("runs", _Run * MAX_ALGOS), ("stats", _Stats)]
 
 
+class _BatchTuning(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_uint32), ("batched_limit", ctypes.c_double)]
+
+
 class _KernelProfile(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint64), ("ms", ctypes.c_double), ("bytes", ctypes.c_double)]
 
@@ -139,6 +143,12 @@ def load_library():
     lib.sw_sort_unique.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U64P, ctypes.c_uint64, _U64P]
     lib.sw_solve_batch.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
                                    ctypes.POINTER(_Result), ctypes.c_uint32]
+    _F64P = ctypes.POINTER(ctypes.c_double)
+    lib.sw_autotune_batch.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
+                                      ctypes.POINTER(_Result), _U32P, ctypes.c_uint32, _F64P, ctypes.c_uint32,
+                                      ctypes.c_uint32, _F64P, ctypes.POINTER(_BatchTuning)]
+    lib.sw_get_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
+    lib.sw_set_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                                      ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_void_p]
@@ -346,12 +356,9 @@ class Context:
         stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
         return Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats)
 
-    def solve_batch(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
-                    workers: int = 0) -> List[Result]:
-        """Solve many automata concurrently (one device stream per worker)."""
+    @staticmethod
+    def _batch_buffers(automata):
         count = len(automata)
-        if count == 0:
-            return []
         ns = np.fromiter((a[0] for a in automata), dtype=np.uint32, count=count)
         ks = np.fromiter((a[1] for a in automata), dtype=np.uint32, count=count)
         total = int(np.dot(ns.astype(np.int64), ks.astype(np.int64)))
@@ -369,16 +376,64 @@ class Context:
         raw[:, o:o + 8] = (np.uint64(words.ctypes.data) + np.uint64(4) * offs[:-1]).view(np.uint8).reshape(count, 8)
         o = _Result.word_capacity.offset
         raw[:, o:o + 4] = caps.astype(np.uint32).view(np.uint8).reshape(count, 4)
-        _check(self._lib.sw_solve_batch(self._h, count, deltas.ctypes.data_as(_U32P), ns.ctypes.data_as(_U32P),
-                                        ks.ctypes.data_as(_U32P), plan_json.encode(), res, workers))
+        return ns, ks, deltas, res, words, offs
+
+    @staticmethod
+    def _batch_results(res, words, offs) -> List[Result]:
         out = []
-        for i in range(count):
+        for i in range(len(res)):
             r = res[i]
             word = words[int(offs[i]): int(offs[i]) + r.word_len].tolist() if r.has_word else None
             runs = [(r.runs[j].name.decode(), r.runs[j].ms) for j in range(r.n_runs)]
             stats = {f: getattr(r.stats, f) for f, _ in _Stats._fields_}
             out.append(Result(bool(r.non_synchro), r.mlsw_lower_bound, r.mlsw_upper_bound, word, runs, stats))
         return out
+
+    def solve_batch(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
+                    workers: int = 0) -> List[Result]:
+        """Solve many automata: a persistent batched launch for small plain-Exact
+        automata, concurrent worker streams for the rest (workers = 0: the
+        autotuned count, else min(count, 16))."""
+        if len(automata) == 0:
+            return []
+        ns, ks, deltas, res, words, offs = self._batch_buffers(automata)
+        _check(self._lib.sw_solve_batch(self._h, len(automata), deltas.ctypes.data_as(_U32P),
+                                        ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P), plan_json.encode(),
+                                        res, workers))
+        return self._batch_results(res, words, offs)
+
+    def autotune_batch(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
+                       workers: Optional[Sequence[int]] = None, limits: Optional[Sequence[float]] = None,
+                       reps: int = 1) -> dict:
+        """Time the batch at each candidate worker count, then at each candidate
+        batched-launch limit (n * log2 k), and keep the fastest as this context's
+        tuning.  Returns {"workers", "batched_limit", "ms": {"workers": {w: ms},
+        "batched_limit": {limit: ms}}}."""
+        if len(automata) == 0:
+            raise ValueError("empty batch")
+        ns, ks, deltas, res, words, offs = self._batch_buffers(automata)
+        wc = _u32(workers if workers is not None else (8, 12, 16, 24))
+        lc = np.ascontiguousarray(np.asarray(limits if limits is not None else (-1.0, 104.0, 1024.0),
+                                             dtype=np.float64))
+        ms = np.zeros(len(wc) + len(lc), dtype=np.float64)
+        best = _BatchTuning()
+        f64 = ctypes.POINTER(ctypes.c_double)
+        _check(self._lib.sw_autotune_batch(self._h, len(automata), deltas.ctypes.data_as(_U32P),
+                                           ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P), plan_json.encode(),
+                                           res, wc.ctypes.data_as(_U32P), len(wc), lc.ctypes.data_as(f64), len(lc),
+                                           reps, ms.ctypes.data_as(f64), ctypes.byref(best)))
+        return {"workers": int(best.workers), "batched_limit": float(best.batched_limit),
+                "ms": {"workers": {int(w): float(t) for w, t in zip(wc, ms[:len(wc)])},
+                       "batched_limit": {float(x): float(t) for x, t in zip(lc, ms[len(wc):])}}}
+
+    def get_batch_tuning(self) -> dict:
+        t = _BatchTuning()
+        _check(self._lib.sw_get_batch_tuning(self._h, ctypes.byref(t)))
+        return {"workers": int(t.workers), "batched_limit": float(t.batched_limit)}
+
+    def set_batch_tuning(self, workers: int = 0, batched_limit: float = 104.0) -> None:
+        t = _BatchTuning(workers, batched_limit)
+        _check(self._lib.sw_set_batch_tuning(self._h, ctypes.byref(t)))
 
     @property
     def stream(self) -> int:

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -34,6 +35,7 @@ struct sw_context {
   std::unique_ptr<sw::Solver> solver;
   std::vector<std::unique_ptr<sw::Solver>> workers;  // extra streams for sw_solve_batch
   SmallBatchState small;
+  sw_batch_tuning tuning{0, 104.0};  // sw_autotune_batch / sw_set_batch_tuning
 };
 
 namespace {
@@ -225,7 +227,7 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     if (count == 0) return SW_OK;
     std::vector<size_t> off(count + 1, 0);
     for (uint32_t i = 0; i < count; ++i) off[i + 1] = off[i] + (size_t)ns[i] * ks[i];
-    if (workers == 0) workers = std::min<uint32_t>(count, 16);
+    if (workers == 0) workers = ctx->tuning.workers ? ctx->tuning.workers : std::min<uint32_t>(count, 16);
     workers = std::max<uint32_t>(1, std::min<uint32_t>(workers, count));
     while (ctx->workers.size() + 1 < workers)
       ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
@@ -251,7 +253,7 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     std::vector<uint32_t> max_len(count, 0);
     for (uint32_t i = 0; i < count; ++i) {
       const uint32_t n = ns[i], k = ks[i];
-      bool ok = n >= 2 && n <= 256 && k >= 1 && k <= 4;
+      bool ok = n >= 2 && n <= 256 && k >= 1 && k <= 4 && (double)n * std::log2((double)k) <= ctx->tuning.batched_limit;
       if (ok) {
         auto key = std::make_pair(n, k);
         auto it = plans.find(key);
@@ -454,6 +456,94 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     if (first_rc.load() != SW_OK) return fail(first_rc.load(), first_err);
     return SW_OK;
   });
+}
+
+int sw_get_batch_tuning(sw_context* ctx, sw_batch_tuning* out) {
+  if (!ctx || !out) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = ctx->tuning;
+  return SW_OK;
+}
+
+int sw_set_batch_tuning(sw_context* ctx, const sw_batch_tuning* in) {
+  if (!ctx || !in) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  ctx->tuning = *in;
+  return SW_OK;
+}
+
+int sw_autotune_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                      const char* plan_json, sw_result* results, const uint32_t* worker_candidates,
+                      uint32_t n_workers, const double* limit_candidates, uint32_t n_limits, uint32_t reps,
+                      double* ms, sw_batch_tuning* best) {
+  if (!ctx || !plan_json || (count && (!deltas || !ns || !ks || !results)))
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (count == 0) return fail(SW_ERR_INVALID_ARGUMENT, "empty batch");
+  static const uint32_t kWorkers[4] = {8, 12, 16, 24};
+  static const double kLimits[3] = {-1.0, 104.0, 1024.0};
+  if (!worker_candidates) {
+    worker_candidates = kWorkers;
+    n_workers = 4;
+  }
+  if (!limit_candidates) {
+    limit_candidates = kLimits;
+    n_limits = 3;
+  }
+  if (n_workers == 0 || n_limits == 0) return fail(SW_ERR_INVALID_ARGUMENT, "empty candidate list");
+  reps = std::max<uint32_t>(reps, 1);
+  const sw_batch_tuning saved = ctx->tuning;
+  // wall-clock time of the batch under tuning t (best of reps)
+  auto run = [&](const sw_batch_tuning& t, double& out) -> int {
+    ctx->tuning = t;
+    for (uint32_t r = 0; r < reps; ++r) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const int rc = sw_solve_batch(ctx, count, deltas, ns, ks, plan_json, results, 0);
+      if (rc != SW_OK) return rc;
+      const double ms_run = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (r == 0 || ms_run < out) out = ms_run;
+    }
+    return SW_OK;
+  };
+  sw_batch_tuning cur = saved, top = saved;
+  double top_ms = 0;
+  bool have = false;
+  for (uint32_t c = 0; c < n_workers; ++c) {
+    cur.workers = std::max<uint32_t>(1, std::min<uint32_t>(worker_candidates[c], count));
+    double t = 0;
+    const int rc = run(cur, t);
+    if (rc != SW_OK) {
+      ctx->tuning = saved;
+      return rc;
+    }
+    if (ms) ms[c] = t;
+    if (!have || t < top_ms) {
+      top_ms = t;
+      top = cur;
+      have = true;
+    }
+  }
+  cur = top;
+  const sw_batch_tuning first = top;
+  const double first_ms = top_ms;
+  for (uint32_t c = 0; c < n_limits; ++c) {
+    cur.batched_limit = limit_candidates[c];
+    if (cur.batched_limit == first.batched_limit) {  // measured in the first pass
+      if (ms) ms[n_workers + c] = first_ms;
+      continue;
+    }
+    double t = 0;
+    const int rc = run(cur, t);
+    if (rc != SW_OK) {
+      ctx->tuning = saved;
+      return rc;
+    }
+    if (ms) ms[n_workers + c] = t;
+    if (t < top_ms) {
+      top_ms = t;
+      top = cur;
+    }
+  }
+  ctx->tuning = top;
+  if (best) *best = top;
+  return SW_OK;
 }
 
 int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const char* plan_json,

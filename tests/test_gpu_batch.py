@@ -27,3 +27,32 @@ def test_batch_4096_lengths_and_words(ctx):
         assert (r.lower, r.upper) == (L, L), (i, n, k, r.lower, r.upper, L)
         assert r.word is not None and len(r.word) == L
         assert len(oracle.apply_word(d, n, k, r.word)) == 1, i
+
+
+def check_against_golden(autos, res):
+    non_sync = set(GOLD["non_synchronizing_indices"])
+    for i, ((n, k, d), r) in enumerate(zip(autos, res)):
+        L = GOLD["lengths"][i]
+        if i in non_sync:
+            assert r.non_synchro, i
+            continue
+        assert (r.lower, r.upper) == (L, L), (i, n, k, r.lower, r.upper, L)
+        assert r.word is not None and len(oracle.apply_word(d, n, k, r.word)) == 1, i
+
+
+def test_autotune_batch_picks_candidates_and_keeps_results(native_lib):
+    import synchrowords_gb300 as sw
+    ctx = sw.Context(0)  # its own context: the tuning stays with it
+    assert ctx.get_batch_tuning() == {"workers": 0, "batched_limit": 104.0}
+    autos = gen.batch(GOLD["count"], GOLD["seed"])[:200]
+    tuned = ctx.autotune_batch(autos, PLAN, workers=(2, 6), limits=(-1.0, 104.0), reps=1)
+    assert tuned["workers"] in (2, 6) and tuned["batched_limit"] in (-1.0, 104.0)
+    assert set(tuned["ms"]["workers"]) == {2, 6} and set(tuned["ms"]["batched_limit"]) == {-1.0, 104.0}
+    assert all(t > 0 for d in tuned["ms"].values() for t in d.values())
+    assert ctx.get_batch_tuning() == {"workers": tuned["workers"], "batched_limit": tuned["batched_limit"]}
+    check_against_golden(autos, ctx.solve_batch(autos, PLAN))  # workers = 0: the tuned count
+    # every route gives the same answers: worker streams only, and the batched launch for all
+    for limit in (-1.0, 1024.0):
+        ctx.set_batch_tuning(workers=4, batched_limit=limit)
+        check_against_golden(autos, ctx.solve_batch(autos, PLAN))
+    ctx.close()
