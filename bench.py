@@ -54,6 +54,13 @@ PLAN_LEARNED_EXACT = json.dumps({
         {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
                                      "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
 
+# the same Exact entry with no beam before it: the plain bidirectional search
+PLAN_PLAIN_EXACT = json.dumps({
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1",
+    "algorithms": [
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
+
 WORKLOADS = {
     # name: (n, k, count, plan, description); n = 0 marks the uneven batch
     "n200": (200, 2, 16, PLAN_EXACT, "plain exact, 16 random binary DFAs, n=200 (256-bit sets)"),
@@ -62,6 +69,8 @@ WORKLOADS = {
                   "plain exact, 4096 random DFAs, n ~ U[32,160], k ~ U{2,3} (64/128/192-bit sets)"),
     "n320": (320, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=320"),
     "n384": (384, 2, 8, PLAN_BEAM_EXACT, "Beam(dynamic)+Exact (configs/exact.json), 8 random binary DFAs, n=384"),
+    "n384_plain": (384, 2, 8, PLAN_PLAIN_EXACT,
+                   "plain Exact (the configs/exact.json Exact entry, no beam), 8 random binary DFAs, n=384"),
     "n384_learned": (384, 2, 8, PLAN_LEARNED_EXACT,
                      "LearnedBeam(4096, distance model)+Exact, 8 random binary DFAs, n=384"),
 }
@@ -69,7 +78,7 @@ WORKLOADS = {
 
 def plan_name(plan: str) -> str:
     return {PLAN_EXACT: "Exact (defaults)", PLAN_BEAM_EXACT: "Beam(dynamic)+Exact",
-            PLAN_LEARNED_EXACT: "LearnedBeam+Exact"}[plan]
+            PLAN_PLAIN_EXACT: "Exact (configs/exact.json entry)", PLAN_LEARNED_EXACT: "LearnedBeam+Exact"}[plan]
 
 
 def workload_dfas(name: str, rank: int):
@@ -176,7 +185,7 @@ def cpu_baseline(dfas, sample: int, threads: int, plan: str = PLAN_EXACT):
     t0 = time.perf_counter()
     lengths = []
     for n, k, d in dfas[:sample]:
-        if plan in (PLAN_BEAM_EXACT, PLAN_LEARNED_EXACT):  # the reference has no learned beam: its own plan
+        if plan in (PLAN_BEAM_EXACT, PLAN_PLAIN_EXACT, PLAN_LEARNED_EXACT):  # at n >= 320: the reference's own plan
             lg = math.log2(n)
             b = oracle.beam(d, n, k, oracle.BeamParams(dynamic=True, presort_indeg=True, min_beam_size=int(n * lg),
                                                        max_beam_size=int(n * n * lg)), upper=(n - 1) ** 2 + 1)
