@@ -277,21 +277,21 @@ class Engine {
     flags_b.reserve(sizeof(u32) * N);
     keep.reserve(sizeof(u32) * N);
     const double t_step0 = vclock();
-    // expansion reads each parent row and writes k child rows
-    timed(1, (double)m * 8.0 * W * (1 + k), [&] {
-      launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream);
-    });
-    launch_iota(ch_vals.as<u32>(), Nc, stream);
-    count_launch(2);
-    if (st) st->subsets_expanded += N;
-    // sort the children by layer key (2 words), then gather the rows in that order
     keys.reserve(sizeof(u64) * 2 * N);
     sorted_rows.reserve(sizeof(u64) * W * N);
-    launch_layer_keys(W, ch_rows.as<u64>(), Nc, keys.as<u64>(), stream, X.keymap);
+    // expansion reads each parent row and writes k child rows, each with its
+    // layer key (2 words) and its index as the sort payload
+    timed(1, (double)m * 8.0 * W * (1 + k) + (double)N * 20.0, [&] {
+      launch_expand(W, forward, X.rows.as<u64>(), m, tables, ch_rows.as<u64>(), stream, keys.as<u64>(),
+                    ch_vals.as<u32>(), X.keymap);
+    });
+    count_launch(1);
+    if (st) st->subsets_expanded += N;
+    // sort the children by layer key, then gather the rows in that order
     sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
     launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
     launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
-    count_launch(3);
+    count_launch(2);
     if (dominance && !self_check && !visited_subsets) {
       // duplicates only: a child is dropped when it equals its predecessor in
       // the sorted layer or a visited set — one flag pass, one compaction
@@ -762,7 +762,10 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     }
     // meet check: some F disjoint from some B-complement (F ⊆ B)
     const double t_meet0 = E.vclock();
-    SW_CUDA(cudaStreamSynchronize(E.stream));
+    // the switch to the bounded phase prices the meet check per query: time it
+    // alone (a synchronisation first) only while that switch is possible
+    const bool time_meet = !bounded && b.has_word;
+    if (time_meet) SW_CUDA(cudaStreamSynchronize(E.stream));
     const auto t_meet_host0 = std::chrono::steady_clock::now();
     SW_CUDA(cudaMemsetAsync(E.d_misc, 0, 4 * sizeof(u32), E.stream));
     E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.B.rows.as<u64>(), E.B.count,

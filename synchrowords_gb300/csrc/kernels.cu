@@ -53,6 +53,38 @@ __device__ __forceinline__ bool row_eq(const u64* a, const u64* b) {
 
 }  // namespace
 
+template <int W>
+__device__ __forceinline__ u64 row_mix(const u64* r, int from) {
+  u64 h = 0x9E3779B97F4A7C15ULL;
+#pragma unroll
+  for (int w = 0; w < W; ++w) {
+    if (w < from) continue;
+    u64 x = r[w] ^ (h + 0x632BE59BD9B4E019ULL * (u64)(w + 1));
+    x ^= x >> 31;
+    x *= 0x94D049BB133111EBULL;
+    x ^= x >> 29;
+    h = (h ^ x) * 0xBF58476D1CE4E5B9ULL;
+  }
+  return (h ^ (h >> 32)) << 32;
+}
+
+template <int W>
+__device__ __forceinline__ void layer_key(const u64* r, const KeyMap& map, u64& k0, u64& k1) {
+  if (map.identity) {
+    k0 = r[0];
+    k1 = W > 1 ? row_mix<W>(r, 1) : 0ULL;
+    return;
+  }
+  u64 a = 0;
+#pragma unroll 8
+  for (int j = 0; j < 64; ++j) {
+    const int q = map.q[j];
+    a |= ((r[q >> 6] >> (63 - (q & 63))) & 1ULL) << (63 - j);
+  }
+  k0 = a;
+  k1 = row_mix<W>(r, 0);
+}
+
 // ===========================================================================
 // Layer expansion.  One warp per input set.  The set row is staged in shared
 // memory; lane l decides output states l, l+32, ... by a gather:
@@ -64,9 +96,11 @@ __device__ __forceinline__ bool row_eq(const u64* a, const u64* b) {
 // ===========================================================================
 template <int W, bool kImage>
 __global__ void __launch_bounds__(256) k_expand(const u64* __restrict__ in, u32 m, TransTables t,
-                                                u64* __restrict__ out) {
+                                                u64* __restrict__ out, u64* __restrict__ keys,
+                                                u32* __restrict__ vals, KeyMap map) {
   extern __shared__ uint16_t s_tab[];
   __shared__ u64 s_row[8][W];
+  __shared__ u64 s_out[8][W];
   const int n = t.n, k = t.k;
   uint16_t* s_a = s_tab;                  // delta (preimage) or inv_beg (image)
   uint16_t* s_b = s_tab + k * (n + 1);    // inv_src (image)
@@ -109,13 +143,27 @@ __global__ void __launch_bounds__(256) k_expand(const u64* __restrict__ in, u32 
           word |= (r & 1) ? v : (v << 32);
         }
       }
-      if (lane < W) out[((size_t)a * m + i) * W + lane] = word;
+      const size_t o = (size_t)a * m + i;
+      if (lane < W) out[o * W + lane] = word;
+      if (keys) {  // the child's layer key and its index as the sort payload
+        if (lane < W) s_out[warp][lane] = word;
+        __syncwarp();
+        if (lane == 0) {
+          u64 k0, k1;
+          layer_key<W>(s_out[warp], map, k0, k1);
+          keys[2 * o] = k0;
+          keys[2 * o + 1] = k1;
+          vals[o] = (u32)o;
+        }
+        __syncwarp();
+      }
     }
     __syncwarp();
   }
 }
 
-void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s) {
+void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s,
+                   u64* keys, u32* vals, const KeyMap& map) {
   if (m == 0) return;
   size_t smem = image ? sizeof(uint16_t) * (size_t)t.k * (2 * t.n + 1) : sizeof(uint16_t) * (size_t)t.k * t.n;
   u32 blocks = std::min<u32>((m + 7) / 8, (u32)sm_count() * 8);
@@ -125,12 +173,12 @@ void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t
       if (smem > 48 * 1024)                                                                         \
         SW_CUDA(cudaFuncSetAttribute(k_expand<WW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)smem));                                                   \
-      k_expand<WW, true><<<blocks, 256, smem, s>>>(in, m, t, out);                                  \
+      k_expand<WW, true><<<blocks, 256, smem, s>>>(in, m, t, out, keys, vals, map);                 \
     } else {                                                                                        \
       if (smem > 48 * 1024)                                                                         \
         SW_CUDA(cudaFuncSetAttribute(k_expand<WW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                                      (int)smem));                                                   \
-      k_expand<WW, false><<<blocks, 256, smem, s>>>(in, m, t, out);                                 \
+      k_expand<WW, false><<<blocks, 256, smem, s>>>(in, m, t, out, keys, vals, map);                \
     }                                                                                               \
     break;
   switch (W) {
@@ -877,38 +925,6 @@ void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, c
 // duplicate in a layer (harmless).  With the identity map the first word is
 // the row's word 0 (states 0..63).
 // ===========================================================================
-template <int W>
-__device__ __forceinline__ u64 row_mix(const u64* r, int from) {
-  u64 h = 0x9E3779B97F4A7C15ULL;
-#pragma unroll
-  for (int w = 0; w < W; ++w) {
-    if (w < from) continue;
-    u64 x = r[w] ^ (h + 0x632BE59BD9B4E019ULL * (u64)(w + 1));
-    x ^= x >> 31;
-    x *= 0x94D049BB133111EBULL;
-    x ^= x >> 29;
-    h = (h ^ x) * 0xBF58476D1CE4E5B9ULL;
-  }
-  return (h ^ (h >> 32)) << 32;
-}
-
-template <int W>
-__device__ __forceinline__ void layer_key(const u64* r, const KeyMap& map, u64& k0, u64& k1) {
-  if (map.identity) {
-    k0 = r[0];
-    k1 = W > 1 ? row_mix<W>(r, 1) : 0ULL;
-    return;
-  }
-  u64 a = 0;
-#pragma unroll 8
-  for (int j = 0; j < 64; ++j) {
-    const int q = map.q[j];
-    a |= ((r[q >> 6] >> (63 - (q & 63))) & 1ULL) << (63 - j);
-  }
-  k0 = a;
-  k1 = row_mix<W>(r, 0);
-}
-
 template <int W>
 __global__ void k_layer_keys(const u64* __restrict__ rows, u32 m, KeyMap map, u64* __restrict__ keys) {
   u32 i = blockIdx.x * blockDim.x + threadIdx.x;

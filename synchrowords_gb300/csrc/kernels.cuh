@@ -27,8 +27,18 @@ struct TransTables {
   int n = 0, k = 0;
 };
 
-// out[(a*m + i)] = image (kImage) or preimage of in[i] under letter a.
-void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s);
+// Sort key of a side: the 64 states whose pattern leads the key (identity =
+// states 0..63, i.e. word 0 of the row).
+struct KeyMap {
+  uint16_t q[64];
+  int identity = 1;
+};
+
+// out[(a*m + i)] = image (kImage) or preimage of in[i] under letter a.  With
+// keys (and vals) given, each child o = a*m + i also gets its layer key
+// keys[2o..2o+1] (as launch_layer_keys with `map`) and vals[o] = o.
+void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t, u64* out, cudaStream_t s,
+                   u64* keys = nullptr, u32* vals = nullptr, const KeyMap& map = KeyMap{});
 
 // Scratch sizing for the sort / scan helpers.
 size_t scan_temp_bytes(u32 n);
@@ -82,13 +92,6 @@ void launch_popcount(int W, const u64* rows, u32 m, u32* out, cudaStream_t s);
 
 // flags[i] = AND/OR combine: out[i] = (a[i] == 0 && b[i] == 0).
 void launch_keep_flags(const u32* a, const u32* b, u32 m, u32* out, cudaStream_t s);
-
-// Sort key of a side: the 64 states whose pattern leads the key (identity =
-// states 0..63, i.e. word 0 of the row).
-struct KeyMap {
-  uint16_t q[64];
-  int identity = 1;
-};
 
 // Layer keys keys[2i..2i+1] = (the map's 64 states of row i packed MSB-first,
 // 32-bit mix of the row in the high half): sort order of a layer and of the
