@@ -45,6 +45,19 @@ def test_version_and_no_device_error(native_lib):
     assert e.value.code == -4  # SW_ERR_NO_DEVICE: no silent CPU path
 
 
+def test_batch_entry_points_reject_null_arguments(native_lib):
+    """The batch and tuning entry points check their pointers before touching
+    a context (so this runs without a GPU) and report through sw_last_error."""
+    lib = native_lib
+    t = sw._BatchTuning(4, 104.0)
+    assert lib.sw_get_batch_tuning(None, ctypes.byref(t)) == -1
+    assert lib.sw_set_batch_tuning(None, ctypes.byref(t)) == -1
+    assert b"NULL" in lib.sw_last_error()
+    assert lib.sw_solve_batch(None, 1, None, None, None, b"{}", None, 0) == -1
+    assert lib.sw_autotune_batch(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
+    assert b"NULL" in lib.sw_last_error()
+
+
 EXPRESSIONS = [
     "AUT_N * 16", "AUT_N * std::log2(AUT_N)", "AUT_N * AUT_N * std::log2(AUT_N)", "1ULL * AUT_N * AUT_N * AUT_N / 6",
     "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1", "12 * 1024", "1024 * 2", "AUT_N * AUT_K", "AUT_N * AUT_K * AUT_K * 8",
