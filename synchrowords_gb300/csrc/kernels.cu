@@ -348,15 +348,19 @@ namespace {
 constexpr int kRsThreads = 256;
 constexpr int kRsRounds = 8;
 constexpr u32 kRsTile = kRsThreads * kRsRounds;
-constexpr int kSmallThreads = 1024;  // shared-memory sorts: 2 ranking rounds for 2048 rows
-constexpr int kSmallRounds = 2;      // rows per thread in a shared-memory sort
+constexpr int kSmallThreads = 1024;  // shared-memory sorts: one compare-exchange per thread per stage
 constexpr u32 kMergeSortMax = 1u << 20;  // up to here: chunk sorts + merge passes; above: radix passes
 
+// Rows of one shared-memory sort: a power of two, at most 2 * kSmallThreads.
 template <int R>
 constexpr u32 small_sort_max() {
   return R <= 4 ? 2048u : 1024u;
 }
-static_assert(2048u <= (u32)kSmallThreads * kSmallRounds, "a shared-memory sort holds its rows in kSmallRounds rounds");
+static_assert(2048u <= 2u * (u32)kSmallThreads, "a shared-memory sort stage is one compare-exchange per thread");
+template <int R>
+constexpr size_t small_sort_smem(u32 rows) {  // keys, payloads, original positions
+  return (size_t)rows * (R * sizeof(u64) + 2 * sizeof(u32));
+}
 
 // Per-round stable ranking inside a 256-thread block.  `d` is this thread's
 // digit (256 = no item).  s_base[256] carries counts of earlier rounds,
@@ -476,152 +480,71 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_downsweep(const u64* __restri
   }
 }
 
-// Whole sort in one block, rows in shared memory (m <= small_sort_max<R>()).
-// block_round_rank for a block of kWarps warps (digit owners: threads < 256).
-template <int kWarps>
-__device__ __forceinline__ u32 block_round_rank_n(u32 d, u32* s_base, u32 (*s_wcnt)[256]) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const u32 peers = __match_any_sync(kFull, d);
-  const u32 lrank = __popc(peers & lanemask_lt());
-#pragma unroll
-  for (int j = 0; j < 8; ++j) s_wcnt[warp][lane * 8 + j] = 0;
-  __syncwarp();
-  if (d < 256 && lrank == 0) s_wcnt[warp][d] = __popc(peers);
-  __syncthreads();
-  if (threadIdx.x < 256) {
-    const int t = threadIdx.x;  // digit owned by this thread
-    u32 run = s_base[t];
-#pragma unroll 8
-    for (int w = 0; w < kWarps; ++w) {
-      u32 c = s_wcnt[w][t];
-      s_wcnt[w][t] = run;
-      run += c;
-    }
-    s_base[t] = run;
-  }
-  __syncthreads();
-  u32 r = (d < 256) ? s_wcnt[warp][d] + lrank : 0;
-  __syncthreads();
-  return r;
-}
-
-// Exclusive prefix sum of h[0..256) in place by the first 256 threads (warp
-// scans, then the 8 warp totals); tmp: 8 words of scratch.  Ends with a
-// block barrier.
-__device__ __forceinline__ void block_exclusive_scan_256(u32* h, u32* tmp) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  u32 v = 0, x = 0;
-  if (threadIdx.x < 256) {
-    v = h[threadIdx.x];
-    x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const u32 y = __shfl_up_sync(kFull, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) tmp[warp] = x;
-  }
-  __syncthreads();
-  if (threadIdx.x < 256) {
-    u32 before = 0;
-    for (int w = 0; w < warp; ++w) before += tmp[w];
-    h[threadIdx.x] = before + x - v;
-  }
-  __syncthreads();
-}
-
+// Whole sort (or one chunk of it) in one block, rows in shared memory
+// (m <= small_sort_max<R>()): a bitonic network over N, the power of two at
+// or above m, padded with rows that order after every real row.  Ties are
+// broken by the row's input position, so the result is the stable order the
+// radix passes and the merge passes assume (equal keys keep their order).
+// N log2(N) (log2(N) + 1) / 4 compare-exchanges, one per thread per stage,
+// a block barrier between stages.
 template <int R>
-__global__ void __launch_bounds__(kSmallThreads) k_rs_small(u64* keys, u32* vals, u32 m_total, u32 chunk) {
+__global__ void __launch_bounds__(kSmallThreads) k_bitonic_small(u64* keys, u32* vals, u32 m_total, u32 chunk) {
   // block b sorts rows [b * chunk, min(m_total, (b + 1) * chunk))
   const u32 base = blockIdx.x * chunk;
   const u32 m = min(chunk, m_total - base);
   keys += (size_t)base * R;
   vals += base;
+  u32 N = 1;
+  while (N < m) N <<= 1;
   extern __shared__ u64 s_mem[];
-  u64* ka = s_mem;
-  u64* kb = ka + (size_t)m * R;
-  u32* va = reinterpret_cast<u32*>(kb + (size_t)m * R);
-  u32* vb = va + m;
-  __shared__ u32 s_hist[256];
-  __shared__ u32 s_base[256];
-  __shared__ u32 s_wcnt[kSmallThreads / 32][256];
-  __shared__ u64 s_or[R], s_and[R];
-  if (threadIdx.x < R) {
-    s_or[threadIdx.x] = 0;
-    s_and[threadIdx.x] = ~0ULL;
+  u64* sk = s_mem;
+  u32* sv = reinterpret_cast<u32*>(sk + (size_t)N * R);
+  u32* sp = sv + N;
+  for (u32 i = threadIdx.x; i < N; i += kSmallThreads) {
+    const bool real = i < m;
+#pragma unroll
+    for (int w = 0; w < R; ++w) sk[(size_t)i * R + w] = real ? keys[(size_t)i * R + w] : ~0ULL;
+    sv[i] = real ? vals[i] : 0xffffffffu;
+    sp[i] = real ? i : 0xffffffffu;
   }
   __syncthreads();
-  {
-    u64 o[R], a[R];
+  for (u32 kk = 2; kk <= N; kk <<= 1) {
+    for (u32 j = kk >> 1; j > 0; j >>= 1) {
+      for (u32 t = threadIdx.x; t < N / 2; t += kSmallThreads) {
+        const u32 lo = ((t & ~(j - 1)) << 1) | (t & (j - 1)), hi = lo + j;
+        u64 a[R], b[R];
 #pragma unroll
-    for (int w = 0; w < R; ++w) {
-      o[w] = 0;
-      a[w] = ~0ULL;
-    }
-    for (u32 i = threadIdx.x; i < m; i += kSmallThreads) {
-#pragma unroll
-      for (int w = 0; w < R; ++w) {
-        u64 v = keys[(size_t)i * R + w];
-        ka[(size_t)i * R + w] = v;
-        o[w] |= v;
-        a[w] &= v;
-      }
-      va[i] = vals[i];
-    }
-#pragma unroll
-    for (int w = 0; w < R; ++w) {
-      atomicOr(&s_or[w], o[w]);
-      atomicAnd(&s_and[w], a[w]);
-    }
-  }
-  __syncthreads();
-  const u32 rounds = (m + kSmallThreads - 1) / kSmallThreads;
-  for (int word = R - 1; word >= 0; --word) {
-    const u64 vary = s_or[word] ^ s_and[word];
-    for (int shift = 0; shift < 64; shift += 8) {
-      if (((vary >> shift) & 255ULL) == 0) continue;
-      // rank every item among equal digits first (the running per-digit
-      // counts end as the digit histogram), then scan the histogram and
-      // scatter: no separate counting pass
-      if (threadIdx.x < 256) s_base[threadIdx.x] = 0;
-      __syncthreads();
-      u32 dr[kSmallRounds], rk[kSmallRounds];
-#pragma unroll
-      for (u32 r = 0; r < (u32)kSmallRounds; ++r) {
-        dr[r] = 256u;
-        rk[r] = 0;
-        if (r < rounds) {
-          const u32 i = r * kSmallThreads + threadIdx.x;
-          dr[r] = i < m ? (u32)((ka[(size_t)i * R + word] >> shift) & 255ULL) : 256u;
-          rk[r] = block_round_rank_n<kSmallThreads / 32>(dr[r], s_base, s_wcnt);
+        for (int w = 0; w < R; ++w) {
+          a[w] = sk[(size_t)lo * R + w];
+          b[w] = sk[(size_t)hi * R + w];
         }
-      }
-      if (threadIdx.x < 256) s_hist[threadIdx.x] = s_base[threadIdx.x];
-      __syncthreads();
-      block_exclusive_scan_256(s_hist, s_wcnt[0]);
+        int cmp = 0;  // sign of a - b, words first, then input position
 #pragma unroll
-      for (u32 r = 0; r < (u32)kSmallRounds; ++r) {
-        if (dr[r] < 256) {
-          const u32 i = r * kSmallThreads + threadIdx.x;
-          const u32 dst = s_hist[dr[r]] + rk[r];
+        for (int w = 0; w < R; ++w)
+          if (cmp == 0 && a[w] != b[w]) cmp = a[w] > b[w] ? 1 : -1;
+        const u32 pa = sp[lo], pb = sp[hi];
+        if (cmp == 0) cmp = pa > pb ? 1 : -1;
+        const bool up = (lo & kk) == 0;  // this pair's run ascends
+        if ((cmp > 0) == up) {
 #pragma unroll
-          for (int w = 0; w < R; ++w) kb[(size_t)dst * R + w] = ka[(size_t)i * R + w];
-          vb[dst] = va[i];
+          for (int w = 0; w < R; ++w) {
+            sk[(size_t)lo * R + w] = b[w];
+            sk[(size_t)hi * R + w] = a[w];
+          }
+          const u32 va = sv[lo];
+          sv[lo] = sv[hi];
+          sv[hi] = va;
+          sp[lo] = pb;
+          sp[hi] = pa;
         }
       }
       __syncthreads();
-      u64* tk = ka;
-      ka = kb;
-      kb = tk;
-      u32* tv = va;
-      va = vb;
-      vb = tv;
     }
   }
   for (u32 i = threadIdx.x; i < m; i += kSmallThreads) {
 #pragma unroll
-    for (int w = 0; w < R; ++w) keys[(size_t)i * R + w] = ka[(size_t)i * R + w];
-    vals[i] = va[i];
+    for (int w = 0; w < R; ++w) keys[(size_t)i * R + w] = sk[(size_t)i * R + w];
+    vals[i] = sv[i];
   }
 }
 
@@ -673,16 +596,17 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
                              int* data_passes) {
   if (data_passes) *data_passes = 0;
   if (m <= 1) return 0;
+  // Raise the shared-memory opt-in once, to the largest size these sorts
+  // use: lowering it per call would race with launches of other host threads.
+  static std::once_flag once;
+  std::call_once(once, [] {
+    SW_CUDA(cudaFuncSetAttribute(k_bitonic_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)small_sort_smem<R>(small_sort_max<R>())));
+  });
   if (m <= small_sort_max<R>()) {
-    size_t smem = (size_t)m * (2 * R * sizeof(u64) + 2 * sizeof(u32));
-    // Raise the opt-in once, to the largest size this path uses: lowering it
-    // per call would race with launches of other host threads.
-    static std::once_flag once;
-    std::call_once(once, [] {
-      const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
-      SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
-    });
-    k_rs_small<R><<<1, kSmallThreads, smem, s>>>(keys, vals, m, m);
+    u32 N = 1;
+    while (N < m) N <<= 1;
+    k_bitonic_small<R><<<1, kSmallThreads, small_sort_smem<R>(N), s>>>(keys, vals, m, m);
     SW_LAUNCH_CHECK();
     if (data_passes) *data_passes = 1;
     return 1;
@@ -693,13 +617,7 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
     // 3-launch pass per key digit
     const u32 chunk = small_sort_max<R>();
     const u32 nchunks = (m + chunk - 1) / chunk;
-    static std::once_flag once2;
-    std::call_once(once2, [] {
-      const int most = (int)(small_sort_max<R>() * (2 * R * sizeof(u64) + 2 * sizeof(u32)));
-      SW_CUDA(cudaFuncSetAttribute(k_rs_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, most));
-    });
-    const size_t smem = (size_t)chunk * (2 * R * sizeof(u64) + 2 * sizeof(u32));
-    k_rs_small<R><<<nchunks, kSmallThreads, smem, s>>>(keys, vals, m, chunk);
+    k_bitonic_small<R><<<nchunks, kSmallThreads, small_sort_smem<R>(chunk), s>>>(keys, vals, m, chunk);
     SW_LAUNCH_CHECK();
     u64 *ki = keys, *ko = keys_alt;
     u32 *vi = vals, *vo = vals_alt;
