@@ -58,6 +58,28 @@ def test_batch_entry_points_reject_null_arguments(native_lib):
     assert b"NULL" in lib.sw_last_error()
 
 
+def test_batch_buffers_layout():
+    """The Python batch wrapper packs the automata back to back and gives
+    result i a word buffer of max(4096, 4 n^2) entries inside one array."""
+    import numpy as np
+    autos = [(3, 2, [1, 2, 0, 0, 2, 1]), (40, 1, list(range(1, 40)) + [0]), (2, 4, [0, 1, 1, 0, 0, 0, 1, 1])]
+    ns, ks, deltas, res, words, offs = sw.Context._batch_buffers(autos)
+    assert ns.tolist() == [3, 40, 2] and ks.tolist() == [2, 1, 4]
+    assert deltas.tolist() == [x for a in autos for x in a[2]]
+    caps = [max(4096, 4 * n * n) for n, _, _ in autos]
+    assert offs.tolist() == [0, caps[0], caps[0] + caps[1], sum(caps)] and words.size == sum(caps)
+    for i, cap in enumerate(caps):
+        assert res[i].word_capacity == cap
+        assert ctypes.addressof(res[i].word.contents) == words.ctypes.data + 4 * int(offs[i])
+    # a result whose word was filled in comes back as that slice
+    words[offs[1]: offs[1] + 3] = [7, 8, 9]
+    res[1].has_word, res[1].word_len, res[1].mlsw_lower_bound, res[1].mlsw_upper_bound = 1, 3, 3, 3
+    out = sw.Context._batch_results(res, words, offs)
+    assert out[1].word == [7, 8, 9] and (out[1].lower, out[1].upper) == (3, 3) and out[0].word is None
+    with pytest.raises(ValueError):
+        sw.Context._batch_buffers([(3, 2, [0, 1, 2])])
+
+
 EXPRESSIONS = [
     "AUT_N * 16", "AUT_N * std::log2(AUT_N)", "AUT_N * AUT_N * std::log2(AUT_N)", "1ULL * AUT_N * AUT_N * AUT_N / 6",
     "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1", "12 * 1024", "1024 * 2", "AUT_N * AUT_K", "AUT_N * AUT_K * AUT_K * 8",
