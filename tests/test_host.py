@@ -157,10 +157,25 @@ def test_plan_evaluation_matches_reference_defines(native_lib):
     assert (ex["max_memory_mb"], ex["dfs_min_list_size"], ex["bfs_small_list_size"]) == (2048, 10000, 3200)
 
 
+def test_learned_beam_plan_entry(native_lib):
+    """LearnedBeam (no reference counterpart): defaults, expressions and the
+    three orders parse; the kind is 6."""
+    d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "LearnedBeam"}]}), 384, 2)["algorithms"][0]
+    assert (d["kind"], d["beam_size"], d["max_iter"], d["order"]) == (6, 4096, -1, 0)
+    for order, code in (("model", 0), ("size", 1), ("size_model", 2)):
+        cfg = {"beam_size": "AUT_N * 16", "max_iter": "AUT_N", "order": order}
+        d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "LearnedBeam", "config": cfg}]}), 320, 2)
+        assert (d["algorithms"][0]["beam_size"], d["algorithms"][0]["max_iter"]) == (5120, 320)
+        assert d["algorithms"][0]["order"] == code
+
+
 @pytest.mark.parametrize("bad", [
     '{"algorithms": []}', '{"algorithms": [{"name": "Nope", "config": {}}]}', '{"threads": 0, "algorithms": '
     '[{"name": "Exact", "config": {}}]}', '{"threads": 65, "algorithms": [{"name": "Exact"}]}',
-    '{"algorithms": [{"name": "Beam", "config": {"presort": "outdeg"}}]}', '{"algorithms": [', 'null'])
+    '{"algorithms": [{"name": "Beam", "config": {"presort": "outdeg"}}]}', '{"algorithms": [', 'null',
+    '{"algorithms": [{"name": "LearnedBeam", "config": {"order": "depth"}}]}',
+    '{"algorithms": [{"name": "LearnedBeam", "config": {"order": 1}}]}',
+    '{"algorithms": [{"name": "LearnedBeam", "config": {"beam_size": "0"}}]}'])
 def test_plan_errors(native_lib, bad):
     with pytest.raises(sw.SynchroError) as e:
         sw.plan_from_json(bad, 10, 2)
