@@ -113,6 +113,65 @@ def test_expression_evaluator_matches_gxx(native_lib, tmp_path, n, k):
             assert int(want_u) == got_u, e
 
 
+def pair_graph_synchronizing(d, n, k):
+    """Every pair of states reaches the diagonal (backward BFS over pairs)."""
+    pre = [[[] for _ in range(k)] for _ in range(n)]
+    for q in range(n):
+        for a in range(k):
+            pre[d[q * k + a]][a].append(q)
+    seen = {(q, q) for q in range(n)}
+    todo = list(seen)
+    while todo:
+        p, q = todo.pop()
+        for a in range(k):
+            for x in pre[p][a]:
+                for y in pre[q][a]:
+                    e = (min(x, y), max(x, y))
+                    if e not in seen:
+                        seen.add(e)
+                        todo.append(e)
+    return len(seen) == n * (n + 1) // 2
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not available")
+def test_host_synchronization_test_matches_pair_graph(tmp_path):
+    """The host-side synchronisation test (csrc/automaton.cpp, used before
+    every streamed solve) agrees with a plain pair-graph BFS on random,
+    one-letter and permutation automata."""
+    import random
+    cuda_inc = next((p for p in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda")
+                     if p and (Path(p) / "include" / "cuda_runtime.h").exists()), None)
+    if cuda_inc is None:
+        pytest.skip("CUDA headers not found")
+    drv = tmp_path / "sync.cpp"
+    drv.write_text('#include <cstdio>\n#include "automaton.hpp"\nint main() {\n  unsigned n, k;\n'
+                   '  while (std::scanf("%u %u", &n, &k) == 2) {\n    std::vector<uint32_t> d(n * k);\n'
+                   '    for (auto& x : d) std::scanf("%u", &x);\n'
+                   '    std::printf("%d\\n", (int)sw::is_synchronizing(sw::make_automaton(d.data(), n, k)));\n'
+                   '  }\n}\n')
+    csrc = ROOT / "synchrowords_gb300" / "csrc"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-w", f"-I{csrc}", f"-I{cuda_inc}/include", str(drv),
+                    str(csrc / "automaton.cpp"), "-o", str(tmp_path / "sync")], check=True)
+    rng = random.Random(3)
+    autos = []
+    for _ in range(300):
+        n, k = rng.randint(1, 30), rng.randint(1, 3)
+        mode = rng.randrange(3)  # 0 random, 1 one permutation letter, 2 all letters permutations
+        d = [0] * (n * k)
+        for a in range(k):
+            perm = list(range(n))
+            rng.shuffle(perm)
+            for q in range(n):
+                d[q * k + a] = perm[q] if mode == 2 or (mode == 1 and a == 0) else rng.randrange(n)
+        autos.append((n, k, d))
+    text = "".join(f"{n} {k} " + " ".join(map(str, d)) + "\n" for n, k, d in autos)
+    out = subprocess.run([str(tmp_path / "sync")], input=text, capture_output=True, text=True, check=True).stdout
+    got = [bool(int(x)) for x in out.split()]
+    want = [pair_graph_synchronizing(d, n, k) for n, k, d in autos]
+    assert got == want
+    assert any(want) and not all(want)
+
+
 def test_expression_errors():
     with pytest.raises(sw.SynchroError):
         sw.eval_expression("AUT_X * 2", 10, 2)
