@@ -134,10 +134,11 @@ def pair_graph_synchronizing(d, n, k):
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="g++ not available")
-def test_host_synchronization_test_matches_pair_graph(tmp_path):
-    """The host-side synchronisation test (csrc/automaton.cpp, used before
-    every streamed solve) agrees with a plain pair-graph BFS on random,
-    one-letter and permutation automata."""
+def test_host_synchronization_test_and_seeds(tmp_path):
+    """The host-side synchronisation test and backward seeds
+    (csrc/automaton.cpp, used before every solve) agree with a plain
+    pair-graph BFS and a reachability restatement on random, one-letter and
+    permutation automata."""
     import random
     cuda_inc = next((p for p in (os.environ.get("CUDA_HOME", ""), "/usr/local/cuda")
                      if p and (Path(p) / "include" / "cuda_runtime.h").exists()), None)
@@ -147,8 +148,10 @@ def test_host_synchronization_test_matches_pair_graph(tmp_path):
     drv.write_text('#include <cstdio>\n#include "automaton.hpp"\nint main() {\n  unsigned n, k;\n'
                    '  while (std::scanf("%u %u", &n, &k) == 2) {\n    std::vector<uint32_t> d(n * k);\n'
                    '    for (auto& x : d) std::scanf("%u", &x);\n'
-                   '    std::printf("%d\\n", (int)sw::is_synchronizing(sw::make_automaton(d.data(), n, k)));\n'
-                   '  }\n}\n')
+                   '    const sw::Automaton A = sw::make_automaton(d.data(), n, k);\n'
+                   '    std::printf("%d", (int)sw::is_synchronizing(A));\n'
+                   '    for (uint32_t q : sw::backward_seeds(A)) std::printf(" %u", q);\n'
+                   '    std::printf("\\n");\n  }\n}\n')
     csrc = ROOT / "synchrowords_gb300" / "csrc"
     subprocess.run(["g++", "-std=c++17", "-O1", "-w", f"-I{csrc}", f"-I{cuda_inc}/include", str(drv),
                     str(csrc / "automaton.cpp"), "-o", str(tmp_path / "sync")], check=True)
@@ -166,10 +169,34 @@ def test_host_synchronization_test_matches_pair_graph(tmp_path):
         autos.append((n, k, d))
     text = "".join(f"{n} {k} " + " ".join(map(str, d)) + "\n" for n, k, d in autos)
     out = subprocess.run([str(tmp_path / "sync")], input=text, capture_output=True, text=True, check=True).stdout
-    got = [bool(int(x)) for x in out.split()]
+    lines = [list(map(int, line.split())) for line in out.strip().split("\n")]
+    got = [bool(line[0]) for line in lines]
     want = [pair_graph_synchronizing(d, n, k) for n, k, d in autos]
     assert got == want
     assert any(want) and not all(want)
+    # backward seeds (exact.cpp:149-164): states of the sink component with a
+    # letter of in-degree > 1; a synchronizing automaton has one sink component
+    for (n, k, d), line, sync in zip(autos, lines, want):
+        if not sync:
+            continue
+        reach = []
+        for q in range(n):
+            seen, todo = {q}, [q]
+            while todo:
+                p = todo.pop()
+                for a in range(k):
+                    t = d[p * k + a]
+                    if t not in seen:
+                        seen.add(t)
+                        todo.append(t)
+            reach.append(seen)
+        sink = [q for q in range(n) if all(q in reach[p] for p in reach[q])]
+        indeg = [[0] * k for _ in range(n)]
+        for q in range(n):
+            for a in range(k):
+                indeg[d[q * k + a]][a] += 1
+        seeds = [q for q in sink if any(indeg[q][a] > 1 for a in range(k))]
+        assert sorted(line[1:]) == seeds, (n, k, d)
 
 
 def test_expression_errors():
