@@ -204,6 +204,50 @@ def fixture_batch(count=4096, seed=2026, sample=24):
                               "reference_checked_indices": checked, "oracle_seconds": round(oracle_s, 1)})
 
 
+def edge_automata():
+    """One-letter and two-state automata, permutation automata (no reset
+    word), Cerny automata up to 24 states, and random automata at every set
+    width boundary from 33 to 256 states."""
+    import random
+    rng = random.Random(77)
+    autos = []
+    for n in (2, 3, 5, 9):
+        for _ in range(3):
+            autos.append((n, 1, [rng.randrange(n) for _ in range(n)]))
+    for k in (1, 2, 3, 4):
+        for _ in range(2):
+            autos.append((2, k, [rng.randrange(2) for _ in range(2 * k)]))
+    for n, k in ((6, 2), (20, 3), (70, 2)):
+        d = [0] * (n * k)
+        for a in range(k):
+            p = list(range(n))
+            rng.shuffle(p)
+            for q in range(n):
+                d[q * k + a] = p[q]
+        autos.append((n, k, d))
+    for n in (5, 12, 20, 24):
+        autos.append((n, 2, gen.cerny(n)))
+    for n, k, s in ((33, 2, 1), (64, 3, 2), (65, 2, 3), (100, 2, 4), (128, 2, 5), (129, 2, 6), (150, 2, 7),
+                    (192, 2, 8), (193, 2, 9), (230, 2, 10), (256, 2, 12), (90, 4, 13)):
+        autos.append((n, k, gen.random_dfa(n, k, 5000 + s)))
+    return autos
+
+
+def fixture_edges():
+    autos = edge_automata()
+    cases = []
+    for n, k, d in autos:
+        res, _ = run_reference(EXACT_DEFAULT, [(n, k, d)])
+        r = res[0]
+        o = oracle.exact(d, n, k)
+        if not r.get("non_synchro"):
+            assert (o.lower, o.upper) == (r["lower"], r["upper"]), (n, k, r, o)
+        cases.append({"n": n, "k": k, "delta": d, "reference": {x: r[x] for x in ("lower", "upper", "non_synchro")
+                                                                 if x in r}})
+    write("batch_edges.json", {"plan": EXACT_DEFAULT, "source": "edge_automata() in make_golden.py",
+                               "cases": cases})
+
+
 EPPSTEIN = {"algorithms": [{"name": "Eppstein", "config": {"find_word": True}}]}
 
 
@@ -310,6 +354,7 @@ def main():
         "eppstein": fixture_eppstein,
         "brute": fixture_brute,
         "reduce": fixture_reduce,
+        "edges": fixture_edges,
     }
     if a.big:
         steps["big"] = fixture_big

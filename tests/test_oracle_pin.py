@@ -139,6 +139,15 @@ def test_oracle_matches_compiled_reference_random_n24():
         assert (o.lower, o.upper) == (r["lower"], r["upper"])
 
 
+def test_oracle_matches_reference_edge_fixture():
+    """One-letter, two-state, permutation, Cerny and width-boundary automata:
+    the oracle's Exact bounds equal the compiled reference's (for automata
+    without a reset word both report the upper bound)."""
+    for c in load("batch_edges.json")["cases"]:
+        o = oracle.exact(c["delta"], c["n"], c["k"])
+        assert (o.lower, o.upper) == (c["reference"]["lower"], c["reference"]["upper"]), (c["n"], c["k"])
+
+
 def test_oracle_eppstein_matches_reference_fixture():
     g = load("eppstein.json")
     for c in g["cases"]:
