@@ -100,8 +100,8 @@ def oracle_beam_exact(d, n, k, threads=1):
     return b.upper, e
 
 
-def write(name: str, obj) -> None:
-    (HERE / name).write_text(json.dumps(obj, indent=1, sort_keys=True) + "\n")
+def write(name: str, obj, compact: bool = False) -> None:
+    (HERE / name).write_text(json.dumps(obj, indent=None if compact else 1, sort_keys=True) + "\n")
     print("wrote", name)
 
 
@@ -201,7 +201,27 @@ def fixture_batch(count=4096, seed=2026, sample=24):
     write("batch_4096.json", {"generator": "batch(4096, 2026): n ~ U[32,160], k ~ U{2,3}", "count": count,
                               "seed": seed, "checksum": checksum(autos), "lengths": lengths,
                               "answers_from": "oracle (trace-identical restatement of the reference)",
-                              "reference_checked_indices": checked, "oracle_seconds": round(oracle_s, 1)})
+                              "reference_checked_indices": checked, "oracle_seconds": round(oracle_s, 1)},
+          compact=True)
+
+
+def fixture_batch_more_checks(extra=104):
+    """Check `extra` more automata of the 4096 batch against the reference
+    binary (spread over (n, k), none checked before) and record them."""
+    path = HERE / "batch_4096.json"
+    g = json.loads(path.read_text())
+    autos = gen.batch(g["count"], g["seed"])
+    assert checksum(autos) == g["checksum"]
+    done = set(g["reference_checked_indices"])
+    order = [i for i in sorted(range(len(autos)), key=lambda i: (autos[i][0], autos[i][1], i)) if i not in done]
+    pick = order[:: max(1, len(order) // extra)][:extra]
+    for i in pick:
+        n, k, d = autos[i]
+        res, _ = run_reference(EXACT_DEFAULT, [(n, k, d)])
+        assert res[0]["lower"] == res[0]["upper"] == g["lengths"][i], (i, res, g["lengths"][i])
+        done.add(i)
+    g["reference_checked_indices"] = sorted(done)
+    write("batch_4096.json", g, compact=True)
 
 
 def edge_automata():
@@ -355,6 +375,7 @@ def main():
         "brute": fixture_brute,
         "reduce": fixture_reduce,
         "edges": fixture_edges,
+        "batchref": fixture_batch_more_checks,
     }
     if a.big:
         steps["big"] = fixture_big
