@@ -1,6 +1,7 @@
 """Exact / Beam parity on the GPU against the oracle (the CPU restatement of the
 reference, itself pinned to the compiled reference) and word verification."""
 import json
+from pathlib import Path
 
 import pytest
 
@@ -187,3 +188,18 @@ def test_solve_batch_concurrent_streams(ctx):
         ref = oracle.exact(d, n, k)
         assert (r.lower, r.upper) == (ref.lower, ref.upper)
         check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("n", [320, 384])
+def test_c5_bench_automata_match_reference(ctx, n):
+    """The eight n = 320 / 384 automata of the bench workloads, solved as the
+    bench solves them (Beam(dynamic)+Exact, concurrent streams): lengths equal
+    the compiled reference's (tests/golden/random_n{320,384}.json) and every
+    word is verified."""
+    g = json.loads((Path(__file__).resolve().parent / "golden" / f"random_n{n}.json").read_text())
+    ref = g["reference"]["beam_exact"]
+    autos = [(n, 2, random_dfa(n, 2, s)) for s in g["seeds"]]
+    res = ctx.solve_batch(autos, json.dumps(ref["plan"]), workers=8)
+    for (nn, k, d), r, want in zip(autos, res, ref["results"]):
+        assert (r.lower, r.upper) == (want["lower"], want["upper"])
+        check_word(d, nn, k, r)
