@@ -1,5 +1,6 @@
 // Batched exact search for small automata: one persistent launch, one block
-// per automaton at a time, every list in shared memory.
+// per automaton at a time; current layers and children in shared memory,
+// visited lists in a per-block global scratch (L2-resident).
 //
 // Blocks take automata from a shared counter until the batch is done.  Each
 // automaton runs the same meet-in-the-middle search as the streamed path
@@ -7,13 +8,14 @@
 // expanded (forward images of F, preimages of the complements B' of the
 // backward sets), the children are sorted (bitonic, in shared memory),
 // children equal to a sibling or to a visited set are dropped (binary search
-// in the side's sorted visited list, kept per block in global memory), the
-// survivors become the side's layer (shared memory) and are merged into its
-// visited list, and the two current layers are meet-checked (f ∩ b' = ∅).  The first length with a meeting pair is the
-// shortest reset length (see the streamed path); the word is traced back
-// through per-layer origin records.  An automaton whose lists outgrow the
-// shared-memory capacities, or whose search reaches the depth limit, is
-// reported as overflowed and solved again by the streamed path.
+// in the side's sorted visited list), the survivors become the side's layer
+// and are merged into its visited list, and the two current layers are
+// meet-checked (f ∩ b' = ∅).  The first length with a meeting pair is the
+// shortest reset length (both sides grow one layer per step and every pair
+// of layer depths is checked once); the word is traced back through
+// per-layer origin records.  An automaton whose lists outgrow the
+// capacities, or whose search reaches the depth or length limit, is reported
+// with the reason and solved again by the streamed path.
 #include <mutex>
 
 #include "algos.cuh"
