@@ -341,8 +341,10 @@ int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32
  * rejected with SW_ERR_CAPACITY.
  *
  * Rows use the device layout: W = ceil(n / 64) uint64 words (1 to 8); state
- * q is bit (63 - q % 64) of word q / 64; unused bits are 0; both row arrays
- * start 16-byte aligned.
+ * q is bit (63 - q % 64) of word q / 64; unused bits are 0.  d_sets must be
+ * 16-byte aligned (its row tiles move as 16-byte loads), d_checks 8-byte and
+ * d_results 4-byte aligned; other pointers are rejected with
+ * SW_ERR_INVALID_ARGUMENT before any work is queued.
  * d_results[i] (uint32) becomes 1 if some d_sets row ⊆ d_checks row i
  * (⊊ when proper), else 0.  The work is queued on `stream` (NULL = default
  * stream); the call returns without waiting for it.  The first call on a

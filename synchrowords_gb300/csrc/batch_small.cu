@@ -355,25 +355,17 @@ size_t small_batch_origin_words(int W, u32 blocks) { return (size_t)blocks * 2 *
 
 size_t small_batch_visited_words(int W, u32 blocks) { return (size_t)blocks * 4 * vis_cap(W) * W; }
 
-int small_batch_blocks() {
-  int dev = 0, sms = 0;
-  SW_CUDA(cudaGetDevice(&dev));
-  SW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  return sms;
-}
+int small_batch_blocks() { return device_sm_count(); }
 
 void launch_small_batch(int W, const SmallInstance* inst, u32 count, const uint8_t* delta_pool,
                         const uint8_t* seed_pool, SmallResult* results, uint8_t* words, u32 word_stride, u32* origins,
                         u64* visited, u32 blocks, u32* counter, cudaStream_t s) {
   if (!count) return;
   SW_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
-  static std::once_flag once;
-  std::call_once(once, [] {
-    SW_CUDA(cudaFuncSetAttribute(k_small_batch<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmCaps<1>::smem));
-    SW_CUDA(cudaFuncSetAttribute(k_small_batch<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmCaps<2>::smem));
-    SW_CUDA(cudaFuncSetAttribute(k_small_batch<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmCaps<3>::smem));
-    SW_CUDA(cudaFuncSetAttribute(k_small_batch<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SmCaps<4>::smem));
-  });
+  ensure_smem_limit((const void*)k_small_batch<1>, (int)SmCaps<1>::smem);
+  ensure_smem_limit((const void*)k_small_batch<2>, (int)SmCaps<2>::smem);
+  ensure_smem_limit((const void*)k_small_batch<3>, (int)SmCaps<3>::smem);
+  ensure_smem_limit((const void*)k_small_batch<4>, (int)SmCaps<4>::smem);
 #define SW_SMALL(WW)                                                                                              \
   k_small_batch<WW><<<blocks, kSmThreads, SmCaps<WW>::smem, s>>>(inst, count, delta_pool, seed_pool, results, words, \
                                                                  word_stride, origins, visited, counter)

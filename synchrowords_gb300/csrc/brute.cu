@@ -88,21 +88,13 @@ size_t brute_visited_bytes(int n) { return n >= 5 ? ((size_t)1 << n) / 8 : 4; }
 
 namespace {
 int brute_grid(u64 work) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    SW_CUDA(cudaGetDevice(&dev));
-    SW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  const int sms = device_sm_count();
   const u64 blocks = (work + kBruteThreads - 1) / kBruteThreads;
   return (int)std::max<u64>(1, std::min<u64>(blocks, (u64)sms * 8));
 }
 void brute_smem_attr() {
-  static std::once_flag once;
-  std::call_once(once, [] {
-    SW_CUDA(cudaFuncSetAttribute(k_brute_level, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxLetters * 4096));
-    SW_CUDA(cudaFuncSetAttribute(k_brute_parent, cudaFuncAttributeMaxDynamicSharedMemorySize, kMaxLetters * 4096));
-  });
+  ensure_smem_limit((const void*)k_brute_level, kMaxLetters * 4096);
+  ensure_smem_limit((const void*)k_brute_parent, kMaxLetters * 4096);
 }
 }  // namespace
 

@@ -54,6 +54,14 @@ __host__ __device__ inline u64 valid_mask(int n, int w) {
   return ~0ULL << (64 - bits);
 }
 
+// Per-device launch facts, looked up once per device and safe to call from
+// several host threads (kernels.cu).  Both act on the current device.
+int device_sm_count();
+// Raises `fn`'s dynamic shared-memory limit to at least `bytes` on the
+// current device.  Limits only grow, so a concurrent launch of `fn` on
+// another host thread never sees its limit lowered below what it asked for.
+void ensure_smem_limit(const void* fn, int bytes);
+
 // Grow-only device buffer (the context keeps them across steps and solves,
 // so a solve performs no per-step cudaMalloc).
 struct DevBuf {

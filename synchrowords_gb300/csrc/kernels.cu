@@ -6,12 +6,44 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "kernels.cuh"
 
 namespace sw {
+
+namespace {
+std::mutex g_devinfo_mu;
+}  // namespace
+
+int device_sm_count() {
+  constexpr int kMaxDev = 64;
+  static int cached[kMaxDev] = {};
+  int dev = 0;
+  SW_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDev) {
+    int sms = 0;
+    SW_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    return sms;
+  }
+  std::lock_guard<std::mutex> g(g_devinfo_mu);
+  if (!cached[dev]) SW_CUDA(cudaDeviceGetAttribute(&cached[dev], cudaDevAttrMultiProcessorCount, dev));
+  return cached[dev];
+}
+
+void ensure_smem_limit(const void* fn, int bytes) {
+  static std::map<std::pair<int, const void*>, int> limits;
+  int dev = 0;
+  SW_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(g_devinfo_mu);
+  int& cur = limits[{dev, fn}];
+  if (bytes <= cur) return;
+  SW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
+}
 
 namespace {
 
@@ -23,15 +55,7 @@ __device__ __forceinline__ u32 lanemask_lt() {
   return m;
 }
 
-int sm_count() {
-  static int cached = 0;
-  if (!cached) {
-    int dev = 0;
-    SW_CUDA(cudaGetDevice(&dev));
-    SW_CUDA(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev));
-  }
-  return cached;
-}
+int sm_count() { return device_sm_count(); }
 
 template <int W>
 __device__ __forceinline__ bool row_less(const u64* a, const u64* b) {
@@ -170,14 +194,10 @@ void launch_expand(int W, bool image, const u64* in, u32 m, const TransTables& t
 #define SW_EXP(WW)                                                                                  \
   case WW:                                                                                          \
     if (image) {                                                                                    \
-      if (smem > 48 * 1024)                                                                         \
-        SW_CUDA(cudaFuncSetAttribute(k_expand<WW, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                     (int)smem));                                                   \
+      if (smem > 48 * 1024) ensure_smem_limit((const void*)k_expand<WW, true>, (int)smem);         \
       k_expand<WW, true><<<blocks, 256, smem, s>>>(in, m, t, out, keys, vals, map);                 \
     } else {                                                                                        \
-      if (smem > 48 * 1024)                                                                         \
-        SW_CUDA(cudaFuncSetAttribute(k_expand<WW, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                                     (int)smem));                                                   \
+      if (smem > 48 * 1024) ensure_smem_limit((const void*)k_expand<WW, false>, (int)smem);        \
       k_expand<WW, false><<<blocks, 256, smem, s>>>(in, m, t, out, keys, vals, map);                \
     }                                                                                               \
     break;
@@ -596,13 +616,10 @@ static int radix_sort_rows_t(u64* keys, u32* vals, u64* keys_alt, u32* vals_alt,
                              int* data_passes) {
   if (data_passes) *data_passes = 0;
   if (m <= 1) return 0;
-  // Raise the shared-memory opt-in once, to the largest size these sorts
-  // use: lowering it per call would race with launches of other host threads.
-  static std::once_flag once;
-  std::call_once(once, [] {
-    SW_CUDA(cudaFuncSetAttribute(k_bitonic_small<R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)small_sort_smem<R>(small_sort_max<R>())));
-  });
+  // Raise the shared-memory opt-in once per device, to the largest size these
+  // sorts use: lowering it per call would race with launches of other host
+  // threads.
+  ensure_smem_limit((const void*)k_bitonic_small<R>, (int)small_sort_smem<R>(small_sort_max<R>()));
   if (m <= small_sort_max<R>()) {
     u32 N = 1;
     while (N < m) N <<= 1;

@@ -101,8 +101,22 @@ extern "C" int sw_subsets_check_device_noalloc(uint32_t n, const uint64_t* d_set
     g_err = "NULL device buffer";
     return SW_ERR_INVALID_ARGUMENT;
   }
+  // the set tiles are copied with 16-byte loads, check rows with 8-byte
+  // loads, results written as 4-byte words: a misaligned pointer would fault
+  // on the GPU, so it is refused here
+  if (((uintptr_t)d_sets & 15u) || ((uintptr_t)d_checks & 7u) || ((uintptr_t)d_results & 3u)) {
+    g_err = "misaligned device buffer: d_sets needs 16-byte, d_checks 8-byte and d_results 4-byte alignment";
+    return SW_ERR_INVALID_ARGUMENT;
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (check_count == 0) return SW_OK;
+  // look the scratch up before queuing anything, so that a failed lookup
+  // returns with the caller's buffers untouched
+  void* scratch = nullptr;
+  if (set_count) {
+    int rc = scratch_address(&scratch, g_err);
+    if (rc != SW_OK) return rc;
+  }
   // results start at zero: the kernel only ever sets flags
   cudaError_t e = cudaMemsetAsync(d_results, 0, sizeof(uint32_t) * check_count, s);
   if (e != cudaSuccess) {
@@ -110,9 +124,6 @@ extern "C" int sw_subsets_check_device_noalloc(uint32_t n, const uint64_t* d_set
     return SW_ERR_CUDA;
   }
   if (set_count == 0) return SW_OK;
-  void* scratch = nullptr;
-  int rc = scratch_address(&scratch, g_err);
-  if (rc != SW_OK) return rc;
   const int W = words_for((int)n);
   auto* masks = static_cast<u64*>(scratch);
   u32* witness = reinterpret_cast<u32*>(masks + kScratchWords - 4);

@@ -35,15 +35,7 @@ constexpr int kWarps = 8;
 constexpr u32 kMinChunkTiles = 4;
 constexpr u32 kFullMask = 0xffffffffu;
 
-int sm_count_sc() {
-  static int cached = 0;
-  if (!cached) {
-    int dev = 0;
-    SW_CUDA(cudaGetDevice(&dev));
-    SW_CUDA(cudaDeviceGetAttribute(&cached, cudaDevAttrMultiProcessorCount, dev));
-  }
-  return cached;
-}
+int sm_count_sc() { return device_sm_count(); }
 
 __host__ __device__ inline u32 n_tiles(u32 m) { return (m + kTileRows - 1) / kTileRows; }
 __host__ __device__ inline u32 n_supers(u32 m) { return (m + kSuperRows - 1) / kSuperRows; }

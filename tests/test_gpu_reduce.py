@@ -113,3 +113,43 @@ def test_cli_readme_run_and_learned_beam(tmp_path):
     r = subprocess.run([str(cli), "-f", str(tmp_path / "in.txt"), "-c", str(tmp_path / "learned.json"), "-q",
                         "-m", str(tmp_path / "missing.f32")], capture_output=True, text=True, timeout=300)
     assert r.returncode == 1
+
+
+def test_cli_continue_resumes_after_the_lines_already_written(tmp_path):
+    """`synchro --continue` (app/main.cpp:25-53): the automata whose result
+    lines are already in the output file (non-empty lines counted) are
+    skipped, and the run appends the rest with their original indices.  The
+    `-b` build suffix is accepted (there is no JIT build to name)."""
+    import subprocess
+    root = Path(__file__).resolve().parents[1]
+    cli = root / "synchrowords_gb300" / "_build" / "synchro"
+    autos = [(30, 2, random_dfa(30, 2, 500 + i)) for i in range(4)]
+    (tmp_path / "in.txt").write_text("".join(f"{k} {n}\n" + " ".join(map(str, d)) + "\n" for n, k, d in autos))
+    (tmp_path / "plan.json").write_text(json.dumps({"algorithms": [{"name": "Exact", "config": {}}]}))
+    base = [str(cli), "-f", str(tmp_path / "in.txt"), "-c", str(tmp_path / "plan.json")]
+    r = subprocess.run(base + ["-o", str(tmp_path / "full.txt"), "-q"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    full = (tmp_path / "full.txt").read_text().splitlines()
+    assert len(full) == 4
+    for i, (n, k, d) in enumerate(autos):
+        o = oracle.exact(d, n, k)
+        assert full[i].startswith(f"{i}: [{o.lower}, {o.upper}] ((Exact, ")
+    # two results already written, then a blank line (not counted)
+    (tmp_path / "out.txt").write_text(full[0] + "\n" + full[1] + "\n\n")
+    r = subprocess.run(base + ["-o", str(tmp_path / "out.txt"), "--continue", "-b", "suffix"], capture_output=True,
+                       text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Skipping 2 automata" in r.stdout + r.stderr
+    got = [s for s in (tmp_path / "out.txt").read_text().splitlines() if s.strip()]
+    assert len(got) == 4
+    assert got[:2] == full[:2]
+    for i in (2, 3):
+        assert got[i].split(" ((")[0] == full[i].split(" ((")[0]  # same index and bounds
+        word = [int(x) for x in got[i].split("{")[1].rstrip("}").split()]
+        n, k, d = autos[i]
+        assert len(oracle.apply_word(d, n, k, word)) == 1  # a reset word (the meeting pair found may differ)
+    # every automaton already has its line: nothing is appended
+    r = subprocess.run(base + ["-o", str(tmp_path / "out.txt"), "--continue", "-q"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert [s for s in (tmp_path / "out.txt").read_text().splitlines() if s.strip()] == got

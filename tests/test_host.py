@@ -58,6 +58,25 @@ def test_batch_entry_points_reject_null_arguments(native_lib):
     assert b"NULL" in lib.sw_last_error()
 
 
+def test_noalloc_rejects_misaligned_buffers_before_any_device_work(native_lib):
+    """The allocation-free subset check validates its pointers on the host: a
+    misaligned set, check or result buffer is refused with
+    SW_ERR_INVALID_ARGUMENT before any CUDA call (so this runs without a GPU;
+    the addresses are never dereferenced)."""
+    lib = native_lib
+    good = 0x10000  # 16-byte aligned, never touched
+    for d_sets, d_checks, d_results in [(good + 8, good, good), (good, good + 4, good), (good, good, good + 2)]:
+        rc = lib.sw_subsets_check_device_noalloc(200, ctypes.c_void_p(d_sets), 10, ctypes.c_void_p(d_checks), 10, 0,
+                                                 ctypes.c_void_p(d_results), None)
+        assert rc == -1, rc  # SW_ERR_INVALID_ARGUMENT
+        assert b"misaligned" in lib.sw_last_error()
+    # 8-byte aligned checks and 4-byte aligned results pass the validation; an
+    # oversized set list is still refused first
+    rc = lib.sw_subsets_check_device_noalloc(64, ctypes.c_void_p(good), (1 << 20) + 1, ctypes.c_void_p(good + 8), 1, 0,
+                                             ctypes.c_void_p(good + 4), None)
+    assert rc == -7  # SW_ERR_CAPACITY
+
+
 def test_batch_buffers_layout():
     """The Python batch wrapper packs the automata back to back and gives
     result i a word buffer of max(4096, 4 n^2) entries inside one array."""

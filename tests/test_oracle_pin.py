@@ -122,7 +122,9 @@ def test_oracle_vs_power_set_bfs(seed):
     assert (o.lower, o.upper) == (truth, truth)
 
 
-REF = Path(os.environ.get("SYNCHRO_REF_ROOT", "/root/reference"))
+# the reference checkout the recipe compiles from (SYNCHRO_REF_ROOT, or the
+# recipe's own default location); absent on machines without it
+from oracle.build_ref import REF_ROOT as REF  # noqa: E402
 
 
 @pytest.mark.skipif(not REF.is_dir(), reason="reference checkout not present")

@@ -71,6 +71,53 @@ def test_noalloc_matches_allocating_entry_point_twice(ctx, native_lib):
         assert 0 < sum(got) < len(got)  # both outcomes occur
 
 
+def device_to_reference_words(rows: np.ndarray) -> np.ndarray:
+    """Bit-reverse every 64-bit word: device layout (state q at bit 63 - q % 64)
+    to the reference layout (state q at bit q % 64)."""
+    rev8 = np.array([int(f"{b:08b}"[::-1], 2) for b in range(256)], dtype=np.uint8)
+    b = np.ascontiguousarray(rows, dtype=np.uint64).view(np.uint8).reshape(-1, 8)
+    return rev8[b[:, ::-1]].copy().view(np.uint64).reshape(rows.shape)
+
+
+def test_noalloc_at_the_maximum_set_count(ctx, native_lib):
+    """Exactly SW_NOALLOC_MAX_SETS sets of 512 states (eight-word rows): the
+    tile and super-tile masks then fill the static scratch to its last word,
+    so an off-by-one in its sizing would show here.  Checked against the
+    allocating entry point on two calls in a row, and on a sample against a
+    numpy restatement."""
+    import torch
+    n, W, m = 512, 8, 1 << 20
+    rng = np.random.default_rng(7)
+    # sets of (at most) 4 random states; a check of density d contains one
+    # with probability about d^4 per set, so at d = 0.01 .. 0.05 over 2^20
+    # sets both outcomes occur
+    S = np.zeros((m, W), dtype=np.uint64)
+    pos = rng.integers(0, n, size=(m, 4))
+    rows = np.repeat(np.arange(m), 4)
+    np.bitwise_or.at(S, (rows, (pos // 64).ravel()), np.uint64(1) << (63 - pos % 64).ravel().astype(np.uint64))
+    dens = np.repeat([0.01, 0.02, 0.03, 0.04, 0.05, 0.3], 400)
+    bits = rng.random((len(dens), n)) < dens[:, None]
+    C = np.packbits(bits.reshape(-1, W, 64), axis=2, bitorder="big").view(">u8").reshape(-1, W).astype(np.uint64)
+    C = np.concatenate([C, S[rng.integers(0, m, size=48)], S[-16:]])  # the last tile's rows are found too
+    want = ctx.subsets_check(n, device_to_reference_words(S), device_to_reference_words(C), proper=False).tolist()
+    ds = torch.from_numpy(S.view(np.int64)).cuda()
+    dc = torch.from_numpy(C.view(np.int64)).cuda()
+    for _ in range(2):
+        res = torch.full((len(C),), 7, dtype=torch.int32, device="cuda")
+        stream = torch.cuda.current_stream()
+        rc = native_lib.sw_subsets_check_device_noalloc(n, ds.data_ptr(), m, dc.data_ptr(), len(C), 0,
+                                                        res.data_ptr(), ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, native_lib.sw_last_error().decode()
+        torch.cuda.synchronize()
+        got = res.cpu().numpy().astype(np.uint8).tolist()
+        assert got == want
+    assert 0 < sum(got) < len(got)
+    assert all(got[-64:])  # the copied sets are always found
+    for i in rng.integers(0, len(C), size=12).tolist():
+        hit = bool(np.any(np.all((S & ~C[i]) == 0, axis=1)))
+        assert got[i] == int(hit), i
+
+
 def test_noalloc_rejects_oversized_set_list(native_lib):
     import torch
     dummy = torch.zeros(8, dtype=torch.int64, device="cuda")
