@@ -206,21 +206,43 @@ int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k
  * reference solves the automata of a file one after another
  * (app/main.cpp:48-78); there is no batched counterpart.
  *
- * Automata of at most 256 states whose plan is a single Exact run and whose
- * n * log2(k) is at most the context's batched_limit (default 104: binary
- * automata up to 104 states, ternary up to 65) are first solved by one
- * persistent batched launch per set width (one GPU block per automaton at a
- * time); those it cannot finish within its capacities, and every other
- * automaton, run on the worker streams.  workers = 0 uses the context's
- * tuned count (sw_autotune_batch / sw_set_batch_tuning), else
- * min(count, 16). */
+ * Automata of at most 256 states (n * k <= 4096) whose plan is a single
+ * Exact run are solved on the device without host round trips:
+ *   - those with n * log2(k) at most the context's batched_limit (default
+ *     104: binary automata up to 104 states, ternary up to 65; k <= 4) by one
+ *     persistent launch per set width, one GPU block per automaton at a time,
+ *     lists in shared memory;
+ *   - the others, and those the first launch cannot finish within its
+ *     capacities, by one persistent launch per set width on thread-block
+ *     clusters (cluster_size CTAs per automaton, lists in the cluster's
+ *     L2-resident global region), unless cluster_size is -1.
+ * What neither finishes within its capacities, and every other automaton,
+ * runs on the worker streams.  workers = 0 uses the context's tuned count
+ * (sw_autotune_batch / sw_set_batch_tuning), else min(count, 16). */
 int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
                    const char* plan_json, sw_result* results, uint32_t workers);
 
 typedef struct {
   uint32_t workers;      /* worker streams when sw_solve_batch gets 0; 0 = min(count, 16) */
   double batched_limit;  /* n * log2(k) bound for the batched launch; < 0 disables it */
+  int32_t cluster_size;  /* CTAs per automaton of the cluster launch (1..16); 0 = 8; -1 disables it */
 } sw_batch_tuning;
+
+/* What the last sw_solve_batch on this context did on the device (no
+ * counterpart in the reference, which solves one automaton at a time). */
+typedef struct {
+  uint32_t small_solved;    /* automata finished by the shared-memory batched launch */
+  uint32_t cluster_solved;  /* automata finished by the cluster launch */
+  uint32_t streamed;        /* automata solved on the worker streams */
+  uint32_t launches;        /* batched kernel launches */
+  double device_ms;         /* CUDA-event time of the batched launches on the batch stream */
+  uint64_t meet_pairs;      /* logical (F, B) pairs of the cluster launches' meet checks */
+  uint64_t children;        /* children expanded by the cluster launches */
+  uint64_t staged_bytes;    /* backward rows the cluster launches' meet checks staged (bit-sliced) on chip */
+  uint64_t steps;           /* BFS levels of the cluster launches */
+} sw_batch_profile;
+
+int sw_batch_last_profile(sw_context* ctx, sw_batch_profile* out);
 
 int sw_get_batch_tuning(sw_context* ctx, sw_batch_tuning* out);
 int sw_set_batch_tuning(sw_context* ctx, const sw_batch_tuning* in);
@@ -228,7 +250,7 @@ int sw_set_batch_tuning(sw_context* ctx, const sw_batch_tuning* in);
 /* Batch autotuner: times the batch (wall clock, best of `reps` runs, 0 = 1)
  * first at each candidate worker count with the current batched_limit, then
  * at each candidate batched_limit with the best worker count, and keeps the
- * fastest pair as the context's tuning.  NULL candidate lists use the
+ * fastest pair as the context's tuning (its cluster_size is kept).  NULL candidate lists use the
  * defaults (workers 8, 12, 16, 24 clipped to count; limits -1, 104, 1024).
  * ms (if not NULL) receives n_workers + n_limits times in that order (4 + 3
  * for the defaults); *best the chosen tuning.  results hold the last run. */

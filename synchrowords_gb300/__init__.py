@@ -100,7 +100,14 @@ class _Result(ctypes.Structure):
 
 
 class _BatchTuning(ctypes.Structure):
-    _fields_ = [("workers", ctypes.c_uint32), ("batched_limit", ctypes.c_double)]
+    _fields_ = [("workers", ctypes.c_uint32), ("batched_limit", ctypes.c_double), ("cluster_size", ctypes.c_int32)]
+
+
+class _BatchProfile(ctypes.Structure):
+    _fields_ = [("small_solved", ctypes.c_uint32), ("cluster_solved", ctypes.c_uint32),
+                ("streamed", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("device_ms", ctypes.c_double),
+                ("meet_pairs", ctypes.c_uint64), ("children", ctypes.c_uint64), ("staged_bytes", ctypes.c_uint64),
+                ("steps", ctypes.c_uint64)]
 
 
 class _KernelProfile(ctypes.Structure):
@@ -149,6 +156,7 @@ def load_library():
                                       ctypes.c_uint32, _F64P, ctypes.POINTER(_BatchTuning)]
     lib.sw_get_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
     lib.sw_set_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
+    lib.sw_batch_last_profile.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchProfile)]
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                                      ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_void_p]
@@ -391,9 +399,11 @@ class Context:
 
     def solve_batch(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
                     workers: int = 0) -> List[Result]:
-        """Solve many automata: a persistent batched launch for small plain-Exact
-        automata, concurrent worker streams for the rest (workers = 0: the
-        autotuned count, else min(count, 16))."""
+        """Solve many automata: plain-Exact automata of up to 256 states are
+        searched on the device (a shared-memory persistent launch for the
+        smallest, a thread-block-cluster launch for the rest), everything else
+        and what those launches cannot finish on concurrent worker streams
+        (workers = 0: the autotuned count, else min(count, 16))."""
         if len(automata) == 0:
             return []
         ns, ks, deltas, res, words, offs = self._batch_buffers(automata)
@@ -423,17 +433,28 @@ class Context:
                                            res, wc.ctypes.data_as(_U32P), len(wc), lc.ctypes.data_as(f64), len(lc),
                                            reps, ms.ctypes.data_as(f64), ctypes.byref(best)))
         return {"workers": int(best.workers), "batched_limit": float(best.batched_limit),
+                "cluster_size": int(best.cluster_size),
                 "ms": {"workers": {int(w): float(t) for w, t in zip(wc, ms[:len(wc)])},
                        "batched_limit": {float(x): float(t) for x, t in zip(lc, ms[len(wc):])}}}
 
     def get_batch_tuning(self) -> dict:
         t = _BatchTuning()
         _check(self._lib.sw_get_batch_tuning(self._h, ctypes.byref(t)))
-        return {"workers": int(t.workers), "batched_limit": float(t.batched_limit)}
+        return {"workers": int(t.workers), "batched_limit": float(t.batched_limit),
+                "cluster_size": int(t.cluster_size)}
 
-    def set_batch_tuning(self, workers: int = 0, batched_limit: float = 104.0) -> None:
-        t = _BatchTuning(workers, batched_limit)
+    def set_batch_tuning(self, workers: int = 0, batched_limit: float = 104.0, cluster_size: int = 0) -> None:
+        """cluster_size: CTAs per automaton of the cluster launch (1..16, 0 = 8, -1 = off)."""
+        t = _BatchTuning(workers, batched_limit, cluster_size)
         _check(self._lib.sw_set_batch_tuning(self._h, ctypes.byref(t)))
+
+    def last_batch_profile(self) -> dict:
+        """What the last solve_batch did on the device: automata per route,
+        batched launches and their CUDA-event milliseconds, and the cluster
+        launches' meet-check pairs, children, staged bytes and levels."""
+        p = _BatchProfile()
+        _check(self._lib.sw_batch_last_profile(self._h, ctypes.byref(p)))
+        return {f: getattr(p, f) for f, _ in _BatchProfile._fields_}
 
     @property
     def stream(self) -> int:

@@ -25,7 +25,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-Wall", "-I", str(ROOT / "include")]
 
-LIB_SOURCES = ["kernels.cu", "subset_check.cu", "noalloc.cu", "pairs.cu", "brute.cu", "batch_small.cu", "mlp.cu",
+LIB_SOURCES = ["kernels.cu", "subset_check.cu", "noalloc.cu", "pairs.cu", "brute.cu", "batch_small.cu",
+               "batch_cluster.cu", "mlp.cu",
                "learn.cu", "exact.cu", "plan.cpp", "automaton.cpp", "abi.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 

@@ -22,10 +22,16 @@
 #include "exact.hpp"
 #include "plan.hpp"
 
-// Device state of the batched small-automaton launch (batch_small.cu).
+// Device state of the batched launches (batch_small.cu, batch_cluster.cu).
 struct SmallBatchState {
   cudaStream_t stream = nullptr;
   sw::DevBuf inst, delta, seeds, results, words, origins, visited, counter;
+  // cluster launch: tag counter, control blocks and per-cluster regions; the
+  // regions' hash tables must start zero-filled (tag 0 = empty slot)
+  sw::DevBuf c_scratch, c_stats;
+  size_t c_zeroed = 0;       // bytes of c_scratch zero-filled since its allocation
+  uint64_t c_tags_used = 0;  // upper bound on the tags taken since the last zero fill
+  sw_batch_profile last{};
   ~SmallBatchState() {
     if (stream) cudaStreamDestroy(stream);
   }
@@ -35,7 +41,7 @@ struct sw_context {
   std::unique_ptr<sw::Solver> solver;
   std::vector<std::unique_ptr<sw::Solver>> workers;  // extra streams for sw_solve_batch
   SmallBatchState small;
-  sw_batch_tuning tuning{0, 104.0};  // sw_autotune_batch / sw_set_batch_tuning
+  sw_batch_tuning tuning{0, 104.0, 0};  // sw_autotune_batch / sw_set_batch_tuning
 };
 
 namespace {
@@ -58,6 +64,8 @@ int guarded(F&& f) {
     return fail(SW_ERR_INVALID_ARGUMENT, e.what());
   } catch (const std::bad_alloc&) {
     return fail(SW_ERR_CAPACITY, "host allocation failed");
+  } catch (const std::length_error& e) {
+    return fail(SW_ERR_CAPACITY, e.what());
   } catch (const std::exception& e) {
     return fail(SW_ERR_INTERNAL, e.what());
   } catch (...) {
@@ -219,18 +227,222 @@ int sw_solve(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, con
   });
 }
 
+namespace {
+
+// One device round of sw_solve_batch: the automata of `small` (shared-memory
+// launch) and `cluster` (cluster launch), each by set width, uploaded once and
+// launched per width on the batch stream; finish_round() waits for it.
+struct DeviceRound {
+  std::vector<uint32_t> order;  // slot -> instance
+  std::vector<uint8_t> engine;  // per slot: 0 shared-memory launch, 1 cluster launch
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int launches = 0;
+  uint32_t word_stride = 1024;
+  bool active = false;
+};
+
+void start_round(sw_context* ctx, DeviceRound& D, const std::vector<uint32_t> small[4],
+                 const std::vector<uint32_t> cluster[4], const uint32_t* deltas, const std::vector<size_t>& off,
+                 const uint32_t* ns, const uint32_t* ks, const std::vector<std::vector<uint32_t>>& seeds,
+                 const std::vector<uint32_t>& max_len) {
+  SmallBatchState& S = ctx->small;
+  size_t total = 0;
+  for (int c = 0; c < 4; ++c) total += small[c].size() + cluster[c].size();
+  if (!total) return;
+  SW_CUDA(cudaSetDevice(ctx->solver->device()));
+  if (!S.stream) SW_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
+  std::vector<sw::SmallInstance> inst;
+  std::vector<uint8_t> dpool, spool;
+  size_t class_start[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int c = 0; c < 8; ++c) {
+    class_start[c] = inst.size();
+    for (uint32_t i : (c < 4 ? small[c] : cluster[c - 4])) {
+      sw::SmallInstance I{ns[i], ks[i], (uint32_t)dpool.size(), (uint32_t)spool.size(), (uint32_t)seeds[i].size(),
+                          std::min<uint32_t>(max_len[i], D.word_stride)};
+      for (size_t e = 0; e < (size_t)ns[i] * ks[i]; ++e) dpool.push_back((uint8_t)deltas[off[i] + e]);
+      for (uint32_t q : seeds[i]) spool.push_back((uint8_t)q);
+      inst.push_back(I);
+      D.order.push_back(i);
+      D.engine.push_back(c < 4 ? 0 : 1);
+    }
+  }
+  class_start[8] = inst.size();
+  S.inst.reserve(sizeof(sw::SmallInstance) * inst.size());
+  S.delta.reserve(std::max<size_t>(dpool.size(), 1));
+  S.seeds.reserve(std::max<size_t>(spool.size(), 1));
+  S.results.reserve(sizeof(sw::SmallResult) * inst.size());
+  S.words.reserve((size_t)D.word_stride * inst.size());
+  S.counter.reserve(sizeof(uint32_t) * 2);
+  const uint32_t blocks = (uint32_t)sw::small_batch_blocks();
+  size_t ow = 0, vw = 0;
+  for (int c = 0; c < 4; ++c)
+    if (!small[c].empty()) {
+      ow = std::max(ow, sw::small_batch_origin_words(c + 1, blocks));
+      vw = std::max(vw, sw::small_batch_visited_words(c + 1, blocks));
+    }
+  if (ow) S.origins.reserve(sizeof(uint32_t) * ow);
+  if (vw) S.visited.reserve(sizeof(uint64_t) * vw);
+  // cluster launch geometry and scratch
+  const int cs = ctx->tuning.cluster_size > 0 ? std::min<int>(ctx->tuning.cluster_size, 16) : 8;
+  const sw::ClusterCaps caps = sw::cluster_default_caps();
+  uint32_t clusters[4] = {0, 0, 0, 0};
+  uint32_t max_clusters = 0;
+  for (int c = 0; c < 4; ++c)
+    if (!cluster[c].empty()) {
+      clusters[c] = std::min<uint32_t>({(uint32_t)cluster[c].size(), sw::cluster_batch_max_clusters(c + 1, cs),
+                                        sw::cluster_max_clusters_supported()});
+      if (!clusters[c]) throw std::runtime_error("cluster launch: no cluster of this size fits on the device");
+      max_clusters = std::max(max_clusters, clusters[c]);
+    }
+  if (max_clusters) {
+    const size_t need = sw::cluster_scratch_bytes(max_clusters, caps);
+    uint64_t tags = 0;
+    for (int c = 0; c < 4; ++c) tags += sw::cluster_tags_per_launch((uint32_t)cluster[c].size());
+    if (S.c_scratch.cap < need) {
+      S.c_scratch.reserve(need);
+      S.c_zeroed = 0;
+    }
+    if (S.c_zeroed < S.c_scratch.cap || S.c_tags_used + tags >= 0xF0000000ull) {
+      // new memory, or the tag counter could wrap: every slot back to "empty"
+      SW_CUDA(cudaMemsetAsync(S.c_scratch.p, 0, S.c_scratch.cap, S.stream));
+      S.c_zeroed = S.c_scratch.cap;
+      S.c_tags_used = 0;
+    }
+    S.c_tags_used += tags;
+    S.c_stats.reserve(sizeof(uint64_t) * 4);
+    SW_CUDA(cudaMemsetAsync(S.c_stats.p, 0, sizeof(uint64_t) * 4, S.stream));
+  }
+  SW_CUDA(cudaMemcpyAsync(S.inst.p, inst.data(), sizeof(sw::SmallInstance) * inst.size(), cudaMemcpyHostToDevice,
+                          S.stream));
+  SW_CUDA(cudaMemcpyAsync(S.delta.p, dpool.data(), dpool.size(), cudaMemcpyHostToDevice, S.stream));
+  SW_CUDA(cudaMemcpyAsync(S.seeds.p, spool.data(), spool.size(), cudaMemcpyHostToDevice, S.stream));
+  SW_CUDA(cudaEventCreate(&D.t0));
+  SW_CUDA(cudaEventCreate(&D.t1));
+  SW_CUDA(cudaEventRecord(D.t0, S.stream));
+  for (int c = 0; c < 8; ++c) {
+    const size_t a = class_start[c], b = class_start[c + 1];
+    if (a == b) continue;
+    ++D.launches;
+    const int W = c % 4 + 1;
+    if (c < 4)
+      sw::launch_small_batch(W, S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a), S.delta.as<uint8_t>(),
+                             S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
+                             S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.origins.as<uint32_t>(),
+                             S.visited.as<sw::u64>(), blocks, S.counter.as<uint32_t>(), S.stream);
+    else
+      sw::launch_cluster_batch(W, cs, clusters[c - 4], S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a),
+                               S.delta.as<uint8_t>(), S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
+                               S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.c_scratch.p, caps,
+                               S.counter.as<uint32_t>(), S.c_stats.as<sw::u64>(), S.stream);
+  }
+  SW_CUDA(cudaEventRecord(D.t1, S.stream));
+  D.active = true;
+}
+
+// Waits for a round, verifies and stores what it solved; returns the
+// instances it did not finish (those of the shared-memory launch go to
+// *unfinished_small when given).
+std::vector<uint32_t> finish_round(sw_context* ctx, DeviceRound& D, const uint32_t* deltas,
+                                   const std::vector<size_t>& off, const uint32_t* ns, const uint32_t* ks,
+                                   const std::map<std::pair<uint32_t, uint32_t>, sw_plan>& plans, sw_result* results,
+                                   std::vector<uint32_t>* unfinished_small, bool verbose) {
+  std::vector<uint32_t> again;
+  if (!D.active) return again;
+  SmallBatchState& S = ctx->small;
+  const size_t m = D.order.size();
+  std::vector<sw::SmallResult> R(m);
+  std::vector<uint8_t> words((size_t)D.word_stride * m);
+  uint64_t cst[4] = {0, 0, 0, 0};
+  SW_CUDA(cudaMemcpyAsync(R.data(), S.results.p, sizeof(sw::SmallResult) * m, cudaMemcpyDeviceToHost, S.stream));
+  SW_CUDA(cudaMemcpyAsync(words.data(), S.words.p, words.size(), cudaMemcpyDeviceToHost, S.stream));
+  const bool any_cluster = std::find(D.engine.begin(), D.engine.end(), 1) != D.engine.end();
+  if (any_cluster) SW_CUDA(cudaMemcpyAsync(cst, S.c_stats.p, sizeof(cst), cudaMemcpyDeviceToHost, S.stream));
+  SW_CUDA(cudaStreamSynchronize(S.stream));
+  float ms = 0;
+  SW_CUDA(cudaEventElapsedTime(&ms, D.t0, D.t1));
+  cudaEventDestroy(D.t0);
+  cudaEventDestroy(D.t1);
+  D.active = false;
+  sw_batch_profile& P = S.last;
+  P.device_ms += ms;
+  P.launches += (uint32_t)D.launches;
+  P.meet_pairs += cst[0];
+  P.children += cst[1];
+  P.staged_bytes += cst[2];
+  P.steps += cst[3];
+  bool first = true;
+  size_t st[2][3] = {{0, 0, 0}, {0, 0, 0}};
+  std::map<std::pair<int, uint32_t>, size_t> over;  // (engine, capacity) -> automata
+  for (size_t t = 0; t < m; ++t) {
+    const uint32_t i = D.order[t];
+    st[D.engine[t]][std::min<uint32_t>(R[t].status, 2)]++;
+    if (R[t].status != 0) {
+      if (R[t].status == 1) over[{D.engine[t], R[t].why & 255u}]++;
+      if (D.engine[t] == 0 && unfinished_small)
+        unfinished_small->push_back(i);
+      else
+        again.push_back(i);
+      continue;
+    }
+    sw_result* r = &results[i];
+    uint32_t* wb = r->word;
+    const uint32_t cap = r->word_capacity;
+    std::memset(r, 0, sizeof(*r));
+    r->word = wb;
+    r->word_capacity = cap;
+    std::vector<uint32_t> word(words.begin() + t * D.word_stride,
+                               words.begin() + t * D.word_stride + R[t].word_len);
+    const sw::Automaton A = sw::make_automaton(deltas + off[i], ns[i], ks[i]);
+    if (word.size() != R[t].length || sw::apply_word(A, word).size() != 1)
+      throw std::runtime_error("internal: batched word does not synchronize");
+    r->mlsw_lower_bound = r->mlsw_upper_bound = R[t].length;
+    r->has_word = 1;
+    r->word_len = R[t].length;
+    if (wb) {
+      if (cap < word.size()) throw std::length_error("instance " + std::to_string(i) + ": word buffer too small");
+      std::memcpy(wb, word.data(), sizeof(uint32_t) * word.size());
+    }
+    const sw_plan& p = plans.at(std::make_pair(ns[i], ks[i]));
+    std::strncpy(r->runs[0].name, p.algorithms[0].name, SW_NAME_LEN - 1);
+    r->runs[0].ms = 0;
+    r->n_runs = 1;
+    r->stats.device_ms = ms / (double)m;
+    if (first) {
+      r->stats.kernel_launches = (uint64_t)D.launches;  // the round's launches, counted once
+      r->stats.meet_pairs = cst[0];
+      r->stats.subsets_expanded = cst[1];
+    }
+    first = false;
+    if (D.engine[t] == 0)
+      P.small_solved++;
+    else
+      P.cluster_solved++;
+  }
+  if (verbose) {
+    for (const auto& kv : over)
+      std::fprintf(stderr, "[sw] %s launch: capacity %u: %zu automata\n", kv.first.first ? "cluster" : "batched",
+                   kv.first.second, kv.second);
+    std::fprintf(stderr,
+                 "[sw] device round: %zu automata in %d launches, %.3f ms; batched launch %zu solved / %zu over "
+                 "capacity / %zu unfinished; cluster launch %zu / %zu / %zu\n",
+                 m, D.launches, (double)ms, st[0][0], st[0][1], st[0][2], st[1][0], st[1][1], st[1][2]);
+  }
+  return again;
+}
+
+}  // namespace
+
 int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
                    const char* plan_json, sw_result* results, uint32_t workers) {
   if (!ctx || !plan_json || (count && (!deltas || !ns || !ks || !results)))
     return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
   return guarded([&] {
+    ctx->small.last = sw_batch_profile{};
     if (count == 0) return SW_OK;
     std::vector<size_t> off(count + 1, 0);
     for (uint32_t i = 0; i < count; ++i) off[i + 1] = off[i] + (size_t)ns[i] * ks[i];
     if (workers == 0) workers = ctx->tuning.workers ? ctx->tuning.workers : std::min<uint32_t>(count, 16);
     workers = std::max<uint32_t>(1, std::min<uint32_t>(workers, count));
-    while (ctx->workers.size() + 1 < workers)
-      ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
     using clk = std::chrono::steady_clock;
     const bool verbose = std::getenv("SYNCHRO_BATCH_VERBOSE") != nullptr;
     const auto h0 = clk::now();
@@ -244,16 +456,19 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
       for (uint32_t w = 1; w < nw; ++w) ctx->workers[w - 1]->set_model(model.data());
       model_copied = true;
     };
-    // Small automata whose plan is a plain Exact run go to one persistent
-    // batched launch (batch_small.cu); the rest, and any automaton that
-    // launch cannot finish, run on the worker streams.
-    std::vector<uint32_t> streamed, small[4];
+    // Automata whose plan is a plain Exact run are searched on the device
+    // without host round trips: the smallest by the shared-memory launch
+    // (batch_small.cu), the others by the cluster launch (batch_cluster.cu).
+    // What neither finishes, and every other automaton, runs on the worker
+    // streams.
+    const bool cluster_on = ctx->tuning.cluster_size >= 0;
+    std::vector<uint32_t> streamed, small[4], cluster[4];
     std::map<std::pair<uint32_t, uint32_t>, sw_plan> plans;
     std::vector<std::vector<uint32_t>> seeds(count);
     std::vector<uint32_t> max_len(count, 0);
     for (uint32_t i = 0; i < count; ++i) {
       const uint32_t n = ns[i], k = ks[i];
-      bool ok = n >= 2 && n <= 256 && k >= 1 && k <= 4 && (double)n * std::log2((double)k) <= ctx->tuning.batched_limit;
+      bool ok = n >= 2 && n <= 256 && k >= 1 && k <= 16 && n * k <= 4096;
       if (ok) {
         auto key = std::make_pair(n, k);
         auto it = plans.find(key);
@@ -265,8 +480,8 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
         const sw_plan& p = it->second;
         ok = p.n_algorithms == 1 && p.algorithms[0].kind == SW_ALGO_EXACT && p.upper_bound >= 1;
         if (ok) {
-          // No synchronisation test here: the batched search reports a length
-          // only when its two sides meet, which proves a reset word; an
+          // No synchronisation test here: the device searches report a length
+          // only when their two sides meet, which proves a reset word; an
           // automaton without one ends over capacity or unfinished and the
           // streamed path settles it.
           const sw::Automaton A = sw::make_automaton(deltas + off[i], n, k);
@@ -274,79 +489,28 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
           std::sort(seeds[i].begin(), seeds[i].end());
           ok = !seeds[i].empty();
           // plain Exact with no word behind the bound searches lengths up to the bound
-          max_len[i] = (uint32_t)std::min<uint64_t>(p.upper_bound, 512);
+          max_len[i] = (uint32_t)std::min<uint64_t>(p.upper_bound, 1024);
         }
       }
-      if (ok)
+      const bool small_ok = ok && k <= 4 && (double)n * std::log2((double)k) <= ctx->tuning.batched_limit;
+      if (small_ok)
         small[(n - 1) / 64].push_back(i);
+      else if (ok && cluster_on)
+        cluster[(n - 1) / 64].push_back(i);
       else
         streamed.push_back(i);
     }
     const double ms_classify = since(h0);
-    SmallBatchState& S = ctx->small;
-    const bool any_small = !small[0].empty() || !small[1].empty() || !small[2].empty() || !small[3].empty();
-    const uint32_t word_stride = 512;
-    cudaEvent_t t0 = nullptr, t1 = nullptr;
-    int small_launches = 0;
-    if (any_small) {
-      SW_CUDA(cudaSetDevice(ctx->solver->device()));
-      if (!S.stream) SW_CUDA(cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking));
-      const uint32_t blocks = (uint32_t)sw::small_batch_blocks();
-      std::vector<sw::SmallInstance> inst;
-      std::vector<uint8_t> dpool, spool;
-      std::vector<uint32_t> order;  // batch slot -> instance
-      size_t class_start[5] = {0, 0, 0, 0, 0};
-      for (int c = 0; c < 4; ++c) {
-        class_start[c] = inst.size();
-        for (uint32_t i : small[c]) {
-          sw::SmallInstance I{ns[i], ks[i], (uint32_t)dpool.size(), (uint32_t)spool.size(),
-                              (uint32_t)seeds[i].size(), max_len[i]};
-          for (size_t e = 0; e < (size_t)ns[i] * ks[i]; ++e) dpool.push_back((uint8_t)deltas[off[i] + e]);
-          for (uint32_t q : seeds[i]) spool.push_back((uint8_t)q);
-          inst.push_back(I);
-          order.push_back(i);
-        }
-      }
-      class_start[4] = inst.size();
-      S.inst.reserve(sizeof(sw::SmallInstance) * inst.size());
-      S.delta.reserve(std::max<size_t>(dpool.size(), 1));
-      S.seeds.reserve(std::max<size_t>(spool.size(), 1));
-      S.results.reserve(sizeof(sw::SmallResult) * inst.size());
-      S.words.reserve((size_t)word_stride * inst.size());
-      size_t ow = 0, vw = 0;
-      for (int c = 0; c < 4; ++c)
-        if (!small[c].empty()) {
-          ow = std::max(ow, sw::small_batch_origin_words(c + 1, blocks));
-          vw = std::max(vw, sw::small_batch_visited_words(c + 1, blocks));
-        }
-      S.origins.reserve(sizeof(uint32_t) * ow);
-      S.visited.reserve(sizeof(uint64_t) * vw);
-      S.counter.reserve(sizeof(uint32_t) * 2);
-      SW_CUDA(cudaMemcpyAsync(S.inst.p, inst.data(), sizeof(sw::SmallInstance) * inst.size(), cudaMemcpyHostToDevice,
-                              S.stream));
-      SW_CUDA(cudaMemcpyAsync(S.delta.p, dpool.data(), dpool.size(), cudaMemcpyHostToDevice, S.stream));
-      SW_CUDA(cudaMemcpyAsync(S.seeds.p, spool.data(), spool.size(), cudaMemcpyHostToDevice, S.stream));
-      SW_CUDA(cudaEventCreate(&t0));
-      SW_CUDA(cudaEventCreate(&t1));
-      SW_CUDA(cudaEventRecord(t0, S.stream));
-      for (int c = 0; c < 4; ++c) {
-        const size_t a = class_start[c], b = class_start[c + 1];
-        if (a == b) continue;
-        ++small_launches;
-        sw::launch_small_batch(c + 1, S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a), S.delta.as<uint8_t>(),
-                               S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
-                               S.words.as<uint8_t>() + a * word_stride, word_stride, S.origins.as<uint32_t>(),
-                               S.visited.as<sw::u64>(), blocks, S.counter.as<uint32_t>(), S.stream);
-      }
-      SW_CUDA(cudaEventRecord(t1, S.stream));
-      // results come back after the streamed instances are done
-      small[0] = order;  // reuse: slot order
-    }
+    DeviceRound round1;
+    start_round(ctx, round1, small, cluster, deltas, off, ns, ks, seeds, max_len);
     std::atomic<int> first_rc{SW_OK};
     std::mutex err_mu;
     std::string first_err;
     auto run_pool = [&](const std::vector<uint32_t>& todo) {
       if (todo.empty()) return;
+      const uint32_t nw = std::min<uint32_t>(workers, (uint32_t)todo.size());
+      while (ctx->workers.size() + 1 < nw) ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
+      ctx->small.last.streamed += (uint32_t)todo.size();
       std::atomic<size_t> next{0};
       auto work = [&](sw::Solver& solver) {
         size_t t;
@@ -377,8 +541,7 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
           }
         }
       };
-      const uint32_t nw = std::min<uint32_t>(workers, (uint32_t)todo.size());
-      copy_model(workers);
+      copy_model(nw);
       std::vector<std::thread> th;
       for (uint32_t w = 1; w < nw; ++w) th.emplace_back(work, std::ref(*ctx->workers[w - 1]));
       work(*ctx->solver);
@@ -388,74 +551,34 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
     const auto h1 = clk::now();
     run_pool(streamed);
     const double ms_streamed = since(h1);
-    if (any_small) {
-      const auto h2 = clk::now();
-      const std::vector<uint32_t>& order = small[0];
-      const size_t m = order.size();
-      std::vector<sw::SmallResult> R(m);
-      std::vector<uint8_t> words((size_t)word_stride * m);
-      SW_CUDA(cudaMemcpyAsync(R.data(), S.results.p, sizeof(sw::SmallResult) * m, cudaMemcpyDeviceToHost, S.stream));
-      SW_CUDA(cudaMemcpyAsync(words.data(), S.words.p, words.size(), cudaMemcpyDeviceToHost, S.stream));
-      SW_CUDA(cudaStreamSynchronize(S.stream));
-      float ms = 0;
-      SW_CUDA(cudaEventElapsedTime(&ms, t0, t1));
-      cudaEventDestroy(t0);
-      cudaEventDestroy(t1);
-      std::vector<uint32_t> again;
-      bool first = true;
-      const double ms_wait = since(h2);
-      for (size_t t = 0; t < m; ++t) {
-        const uint32_t i = order[t];
-        if (R[t].status != 0) {
-          again.push_back(i);
-          continue;
-        }
-        sw_result* r = &results[i];
-        uint32_t* wb = r->word;
-        const uint32_t cap = r->word_capacity;
-        std::memset(r, 0, sizeof(*r));
-        r->word = wb;
-        r->word_capacity = cap;
-        std::vector<uint32_t> word(words.begin() + t * word_stride, words.begin() + t * word_stride + R[t].word_len);
-        const sw::Automaton A = sw::make_automaton(deltas + off[i], ns[i], ks[i]);
-        if (word.size() != R[t].length || sw::apply_word(A, word).size() != 1)
-          throw std::runtime_error("internal: batched word does not synchronize");
-        r->mlsw_lower_bound = r->mlsw_upper_bound = R[t].length;
-        r->has_word = 1;
-        r->word_len = R[t].length;
-        if (wb) {
-          if (cap < word.size()) return fail(SW_ERR_CAPACITY, "instance " + std::to_string(i) + ": word buffer too small");
-          std::memcpy(wb, word.data(), sizeof(uint32_t) * word.size());
-        }
-        const sw_plan& p = plans.at(std::make_pair(ns[i], ks[i]));
-        std::strncpy(r->runs[0].name, p.algorithms[0].name, SW_NAME_LEN - 1);
-        r->runs[0].ms = 0;
-        r->n_runs = 1;
-        r->stats.device_ms = ms / (double)m;
-        if (first) r->stats.kernel_launches = (uint64_t)small_launches;  // the batch's launches, counted once
-        first = false;
-      }
-      const double ms_results = since(h2) - ms_wait;
-      if (verbose) {
-        size_t st[3] = {0, 0, 0};
-        std::map<std::pair<uint32_t, uint32_t>, size_t> over;  // (capacity, set width) -> automata
-        for (size_t t = 0; t < m; ++t) {
-          st[std::min<uint32_t>(R[t].status, 2)]++;
-          if (R[t].status == 1) over[{R[t].why & 255u, (ns[order[t]] + 63) / 64}]++;
-        }
-        for (const auto& kv : over)
-          std::fprintf(stderr, "[sw] batched launch: capacity %u (W=%u): %zu automata\n", kv.first.first,
-                       kv.first.second, kv.second);
-        std::fprintf(stderr,
-                     "[sw] batched launch: %zu automata, %zu solved, %zu over capacity, %zu unfinished, %.3f ms on "
-                     "the device; host: classify %.3f, upload+launch %.3f, streamed %.3f, wait %.3f, results %.3f ms\n",
-                     m, st[0], st[1], st[2], (double)ms, ms_classify, ms_launch, ms_streamed, ms_wait, ms_results);
-      }
-      run_pool(again);
+    const auto h2 = clk::now();
+    // what the shared-memory launch leaves gets a cluster round before the streams
+    std::vector<uint32_t> small_left;
+    std::vector<uint32_t> again = finish_round(ctx, round1, deltas, off, ns, ks, plans, results,
+                                               cluster_on ? &small_left : nullptr, verbose);
+    if (!small_left.empty()) {
+      std::vector<uint32_t> none[4], second[4];
+      for (uint32_t i : small_left) second[(ns[i] - 1) / 64].push_back(i);
+      DeviceRound round2;
+      start_round(ctx, round2, none, second, deltas, off, ns, ks, seeds, max_len);
+      std::vector<uint32_t> left = finish_round(ctx, round2, deltas, off, ns, ks, plans, results, nullptr, verbose);
+      again.insert(again.end(), left.begin(), left.end());
     }
+    const double ms_device = since(h2);
+    if (verbose)
+      std::fprintf(stderr, "[sw] batch of %u: host classify %.3f ms, upload+launch %.3f ms, streamed %.3f ms, "
+                   "device rounds %.3f ms, %zu left for the streams\n", count, ms_classify, ms_launch, ms_streamed,
+                   ms_device, again.size());
+    run_pool(again);
     if (first_rc.load() != SW_OK) return fail(first_rc.load(), first_err);
     return SW_OK;
   });
+}
+
+int sw_batch_last_profile(sw_context* ctx, sw_batch_profile* out) {
+  if (!ctx || !out) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = ctx->small.last;
+  return SW_OK;
 }
 
 int sw_get_batch_tuning(sw_context* ctx, sw_batch_tuning* out) {

@@ -72,4 +72,29 @@ void launch_small_batch(int W, const SmallInstance* inst, u32 count, const uint8
                         const uint8_t* seed_pool, SmallResult* results, uint8_t* words, u32 word_stride, u32* origins,
                         u64* visited, u32 blocks, u32* counter, cudaStream_t s);
 
+// Device-resident search on thread-block clusters (batch_cluster.cu): one
+// cluster of `cs` CTAs per automaton (n <= 256, n * k <= 4096), lists in a
+// per-cluster global region.  Same instances and results as the small batch;
+// status 1 may also report why 6 (a hash-table probe ran out).
+struct ClusterCaps {
+  u32 vis = 0;        // visited rows per side (every layer of the side, in order)
+  u32 ch = 0;         // children of one step
+  u32 vtab_bits = 0;  // log2 slots of a side's visited table (>= 2 * vis)
+  u32 ltab_bits = 0;  // log2 slots of the step's child table (>= 2 * ch)
+};
+ClusterCaps cluster_default_caps();
+// Bytes of scratch for `clusters` clusters.  It must be zero-filled before its
+// first launch, and again before the tags the launches take from its counter
+// (cluster_tags_per_launch) could wrap around 2^32.
+size_t cluster_scratch_bytes(u32 clusters, const ClusterCaps& c);
+u32 cluster_max_clusters_supported();
+// Clusters of `cs` CTAs that fit on the current device at once.
+u32 cluster_batch_max_clusters(int W, int cs);
+// Tags a launch of `count` automata can take: one per search, one per step.
+constexpr u64 cluster_tags_per_launch(u32 count) { return (u64)count * (2 + 2 * 1024); }
+void launch_cluster_batch(int W, int cs, u32 clusters, const SmallInstance* inst, u32 count,
+                          const uint8_t* delta_pool, const uint8_t* seed_pool, SmallResult* results, uint8_t* words,
+                          u32 word_stride, void* scratch, const ClusterCaps& caps, u32* counter, u64* stats,
+                          cudaStream_t s);
+
 }  // namespace sw

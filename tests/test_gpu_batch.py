@@ -1,5 +1,6 @@
 """Uneven batch of 4096 random automata, n ~ U[32,160], k ~ U{2,3}, solved
-through sw_solve_batch (batched launch plus worker streams); every length equals the
+through sw_solve_batch (the shared-memory batched launch, the cluster launch
+and worker streams); every length equals the
 committed golden (oracle, spot-checked against the compiled reference) and every
 word is verified."""
 import json
@@ -19,6 +20,9 @@ PLAN = json.dumps({"algorithms": [{"name": "Exact", "config": {}}]})
 def test_batch_4096_lengths_and_words(ctx):
     autos = gen.batch(GOLD["count"], GOLD["seed"])
     res = ctx.solve_batch(autos, PLAN, workers=16)
+    prof = ctx.last_batch_profile()
+    # with the default tuning both device launches take part and the streams see only leftovers
+    assert prof["small_solved"] > 1000 and prof["cluster_solved"] > 1000, prof
     non_sync = set(GOLD["non_synchronizing_indices"])
     for i, ((n, k, d), r, L) in enumerate(zip(autos, res, GOLD["lengths"])):
         if i in non_sync:
@@ -43,16 +47,21 @@ def check_against_golden(autos, res):
 def test_autotune_batch_picks_candidates_and_keeps_results(native_lib):
     import synchrowords_gb300 as sw
     ctx = sw.Context(0)  # its own context: the tuning stays with it
-    assert ctx.get_batch_tuning() == {"workers": 0, "batched_limit": 104.0}
+    assert ctx.get_batch_tuning() == {"workers": 0, "batched_limit": 104.0, "cluster_size": 0}
     autos = gen.batch(GOLD["count"], GOLD["seed"])[:200]
     tuned = ctx.autotune_batch(autos, PLAN, workers=(2, 6), limits=(-1.0, 104.0), reps=1)
     assert tuned["workers"] in (2, 6) and tuned["batched_limit"] in (-1.0, 104.0)
     assert set(tuned["ms"]["workers"]) == {2, 6} and set(tuned["ms"]["batched_limit"]) == {-1.0, 104.0}
     assert all(t > 0 for d in tuned["ms"].values() for t in d.values())
-    assert ctx.get_batch_tuning() == {"workers": tuned["workers"], "batched_limit": tuned["batched_limit"]}
+    assert ctx.get_batch_tuning() == {"workers": tuned["workers"], "batched_limit": tuned["batched_limit"],
+                                      "cluster_size": 0}
     check_against_golden(autos, ctx.solve_batch(autos, PLAN))  # workers = 0: the tuned count
-    # every route gives the same answers: worker streams only, and the batched launch for all
-    for limit in (-1.0, 1024.0):
-        ctx.set_batch_tuning(workers=4, batched_limit=limit)
+    # every route gives the same answers: worker streams only, the shared-memory
+    # launch for all it accepts, the cluster launch for all, and clusters of 4 and 16 CTAs
+    for limit, cs in ((-1.0, -1), (1024.0, -1), (-1.0, 0), (-1.0, 4), (-1.0, 16)):
+        ctx.set_batch_tuning(workers=4, batched_limit=limit, cluster_size=cs)
         check_against_golden(autos, ctx.solve_batch(autos, PLAN))
+        prof = ctx.last_batch_profile()
+        if cs >= 0:
+            assert prof["cluster_solved"] > 0 and prof["small_solved"] == 0, prof
     ctx.close()

@@ -5,8 +5,9 @@ whose searches are deep (up to 361 letters, and one past the launch's
 512-letter search bound), every set width 1..4 in one batch, and automata
 whose layers outgrow the launch's capacities.  Each batch is solved with the
 batched launch taking every automaton it accepts (batched_limit 1024) and
-with the launch turned off (batched_limit -1): both routes must give the
-reference's lengths and verified words.  The reference's Exact has no
+with the launch turned off (batched_limit -1), each with the cluster launch
+(k_cluster_batch: clusters of 8 or 2 CTAs) on or off: every route must give
+the reference's lengths and verified words.  The reference's Exact has no
 synchronisation test (it reports its upper bound for an automaton without a
 reset word); the library reports non_synchro there, checked against a
 pair-graph BFS."""
@@ -47,14 +48,14 @@ def synchronizing(d, n, k):
     return reached == n * (n + 1) // 2
 
 
-@pytest.mark.parametrize("limit", [1024.0, -1.0])
-def test_batched_launch_edges_match_reference(native_lib, limit):
+@pytest.mark.parametrize("limit,cluster", [(1024.0, -1), (-1.0, -1), (-1.0, 0), (1024.0, 0), (-1.0, 2)])
+def test_batched_launch_edges_match_reference(native_lib, limit, cluster):
     import synchrowords_gb300 as sw
     autos = [(c["n"], c["k"], c["delta"]) for c in GOLD["cases"]]
     sync = [synchronizing(d, n, k) for n, k, d in autos]
     assert any(sync) and not all(sync)
     with sw.Context(0) as ctx:
-        ctx.set_batch_tuning(workers=4, batched_limit=limit)
+        ctx.set_batch_tuning(workers=4, batched_limit=limit, cluster_size=cluster)
         res = ctx.solve_batch(autos, PLAN)
     for i, ((n, k, d), r, s, c) in enumerate(zip(autos, res, sync, GOLD["cases"])):
         assert r.non_synchro == (not s), (i, n, k)

@@ -203,3 +203,85 @@ def test_c5_bench_automata_match_reference(ctx, n):
     for (nn, k, d), r, want in zip(autos, res, ref["results"]):
         assert (r.lower, r.upper) == (want["lower"], want["upper"])
         check_word(d, nn, k, r)
+
+
+def _fixture(name):
+    return json.loads((Path(__file__).resolve().parent / "golden" / name).read_text())
+
+
+@pytest.mark.parametrize("limit,cluster", [(104.0, 0), (-1.0, 0), (-1.0, -1)])
+def test_c1_all_64_through_solve_batch_match_reference(native_lib, limit, cluster):
+    """All 64 n = 48 automata of tests/golden/random_n48.json (the compiled
+    reference's Exact lengths) through sw_solve_batch on each route: the
+    shared-memory batched launch (the default for n = 48, as the bench's n48
+    workload runs them), the cluster launch, and the worker streams."""
+    import synchrowords_gb300 as sw
+    g = _fixture("random_n48.json")
+    want = g["reference"]["exact_default"]["results"]
+    autos = [(48, 2, random_dfa(48, 2, s)) for s in g["seeds"]]
+    assert len(autos) == 64
+    with sw.Context(0) as c:
+        c.set_batch_tuning(workers=8, batched_limit=limit, cluster_size=cluster)
+        res = c.solve_batch(autos, EXACT)
+        prof = c.last_batch_profile()
+    if limit > 0:
+        assert prof["small_solved"] == 64
+    elif cluster >= 0:
+        assert prof["cluster_solved"] == 64
+    else:
+        assert prof["streamed"] == 64
+    for (n, k, d), r, w in zip(autos, res, want):
+        assert (r.lower, r.upper) == (w["lower"], w["upper"])
+        check_word(d, n, k, r)
+
+
+@pytest.mark.parametrize("cluster", [0, 4, 16])
+def test_c2_n200_cluster_launch_matches_reference(native_lib, cluster):
+    """The sixteen n = 200 automata of the bench workload
+    (tests/golden/random_n200.json, the compiled reference's plain Exact
+    lengths) solved by the cluster launch alone: one cluster of 8 (default), 4
+    or 16 CTAs per automaton, the whole search in one launch."""
+    import synchrowords_gb300 as sw
+    g = _fixture("random_n200.json")
+    want = g["reference"]["exact_default"]["results"]
+    autos = [(200, 2, random_dfa(200, 2, s)) for s in g["seeds"]]
+    with sw.Context(0) as c:
+        c.set_batch_tuning(workers=16, batched_limit=104.0, cluster_size=cluster)
+        res = c.solve_batch(autos, EXACT)
+        prof = c.last_batch_profile()
+    assert prof["cluster_solved"] == 16 and prof["streamed"] == 0, prof
+    assert prof["launches"] == 1 and prof["device_ms"] > 0
+    for (n, k, d), r, w in zip(autos, res, want):
+        assert (r.lower, r.upper) == (w["lower"], w["upper"])
+        check_word(d, n, k, r)
+
+
+def test_cluster_launch_random_sizes_against_the_streamed_path(native_lib):
+    """Uneven sizes across every set width of the cluster launch (n = 2..256,
+    k = 1..16), against the streamed path (itself checked against the oracle
+    and the reference's fixtures) and, for n <= 65, against the oracle;
+    automata without a reset word fall through to the streamed path and are
+    reported as such."""
+    import random
+    import synchrowords_gb300 as sw
+    rng = random.Random(77)
+    autos = []
+    for i in range(48):
+        n = rng.choice([2, 3, 17, 63, 64, 65, 100, 128, 129, 150, 192, 193, 230, 256])
+        k = rng.choice([kk for kk in (1, 2, 3, 4, 7, 16) if n * kk <= (4096 if kk <= 2 else 700)])
+        autos.append((n, k, random_dfa(n, k, 4000 + i)))
+    with sw.Context(0) as c:
+        c.set_batch_tuning(workers=8, batched_limit=-1.0, cluster_size=0)
+        res = c.solve_batch(autos, EXACT)
+        prof = c.last_batch_profile()
+        c.set_batch_tuning(workers=8, batched_limit=-1.0, cluster_size=-1)
+        streamed = c.solve_batch(autos, EXACT)
+    assert prof["cluster_solved"] > 24, prof
+    for (n, k, d), r, s in zip(autos, res, streamed):
+        assert (r.non_synchro, r.lower, r.upper) == (s.non_synchro, s.lower, s.upper), (n, k)
+        if r.non_synchro:
+            continue  # the reference's Exact has no such test: it reports its upper bound
+        if n <= 65:
+            ref = oracle.exact(d, n, k)
+            assert (r.lower, r.upper) == (ref.lower, ref.upper), (n, k)
+        check_word(d, n, k, r)
