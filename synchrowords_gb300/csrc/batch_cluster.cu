@@ -49,7 +49,7 @@ constexpr int kCtWarps = kCtThreads / 32;
 constexpr u32 kCtMaxDepth = 1024;   // layers per side
 constexpr u32 kCtChunkRows = 4096;  // backward rows per bit-sliced meet-check chunk
 constexpr u32 kCtGroups = kCtChunkRows / 32;  // 32-row bitmap words per state and chunk
-constexpr u32 kCtFSlice = 1024;     // forward sets per meet-check unit (32 per warp)
+constexpr u32 kCtFSlice = 32 * kCtWarps;  // forward sets per meet-check unit (32 per warp)
 constexpr u32 kCtMaxNK = 4096;      // n * k of the transition table staged per CTA
 constexpr u32 kRunning = 255;
 
@@ -465,27 +465,35 @@ __global__ void __launch_bounds__(kCtThreads, 1)
           my_staged += (u64)rows * W * 8;
           __syncthreads();
         }
-        // warp per forward set: AND the bitmaps of its states, lane l owns
-        // words l, l + 32, l + 64, l + 96 of the chunk
-        const u32 f0 = fs * kCtFSlice, f1 = min(nF, f0 + kCtFSlice);
-        bool done = false;
-        for (u32 fi = f0 + warp; fi < f1 && !done; fi += kCtWarps) {
-          u32 acc[4];
+        // warp per 32 forward sets: lane l fetches set f0 + 32 warp + l, then
+        // the warp takes them one by one (broadcast by shuffle) and ANDs the
+        // bitmaps of each set's states; lane l owns the chunk's 32-row words
+        // 4l .. 4l + 3 (one 16-byte shared load per state)
+        const u32 fw0 = fs * kCtFSlice + warp * 32;
+        const u32 fw1 = min(nF, fw0 + 32);
+        u64 myf[W];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const u32 g = lane + 32 * i;
-            acc[i] = g < groups ? (32 * g + 32 <= rows ? 0xffffffffu : (1u << (rows - 32 * g)) - 1u) : 0u;
-          }
+        for (int w = 0; w < W; ++w) myf[w] = fw0 + lane < fw1 ? Frows[(size_t)(fw0 + lane) * W + w] : 0ULL;
+        u32 acc0[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const u32 g = 4 * lane + i;
+          acc0[i] = g < groups ? (32 * g + 32 <= rows ? 0xffffffffu : (1u << (rows - 32 * g)) - 1u) : 0u;
+        }
+        for (u32 t = 0; fw0 + t < fw1; ++t) {
+          u32 acc[4] = {acc0[0], acc0[1], acc0[2], acc0[3]};
           bool alive = true;
 #pragma unroll
           for (int w = 0; w < W; ++w) {
-            u64 v = Frows[(size_t)fi * W + w];
+            u64 v = __shfl_sync(0xffffffffu, myf[w], t);
             while (v && alive) {
               const u32 j = __clzll((long long)v);  // state 64 w + j (bit 63 - j)
               v &= ~(0x8000000000000000ULL >> j);
-              const u32* colq = s_col + (64 * w + j) * kCtGroups;
-#pragma unroll
-              for (int i = 0; i < 4; ++i) acc[i] &= colq[(lane + 32 * i) & (kCtGroups - 1)];
+              const uint4 col = reinterpret_cast<const uint4*>(s_col + (64 * w + j) * kCtGroups)[lane];
+              acc[0] &= col.x;
+              acc[1] &= col.y;
+              acc[2] &= col.z;
+              acc[3] &= col.w;
               alive = __any_sync(0xffffffffu, (acc[0] | acc[1] | acc[2] | acc[3]) != 0u);
             }
           }
@@ -493,14 +501,14 @@ __global__ void __launch_bounds__(kCtThreads, 1)
             u32 hit = 0xffffffffu;
 #pragma unroll
             for (int i = 3; i >= 0; --i)
-              if (acc[i]) hit = 32 * (lane + 32 * i) + __ffs(acc[i]) - 1;
+              if (acc[i]) hit = 32 * (4 * lane + i) + __ffs(acc[i]) - 1;
             const u32 who = __ballot_sync(0xffffffffu, hit != 0xffffffffu);
             const u32 bj = __shfl_sync(0xffffffffu, hit, __ffs(who) - 1);
             if (lane == 0 && atomicCAS(&ctl->found, 0u, 1u) == 0u) {
-              ctl->fi = fi;
+              ctl->fi = fw0 + t;
               ctl->bj = r0 + bj;
             }
-            done = true;
+            break;
           }
         }
         __syncthreads();  // the staged chunk stays until every warp is done with it
