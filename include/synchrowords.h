@@ -215,7 +215,8 @@ int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k
  *   - the others, and those the first launch cannot finish within its
  *     capacities, by one persistent launch per set width on thread-block
  *     clusters (cluster_size CTAs per automaton, lists in the cluster's
- *     L2-resident global region), unless cluster_size is -1.
+ *     L2-resident global region) when n * log2(k) is at most cluster_limit
+ *     (and cluster_size is not -1).
  * What neither finishes within its capacities, and every other automaton,
  * runs on the worker streams.  workers = 0 uses the context's tuned count
  * (sw_autotune_batch / sw_set_batch_tuning), else min(count, 16). */
@@ -226,6 +227,7 @@ typedef struct {
   uint32_t workers;      /* worker streams when sw_solve_batch gets 0; 0 = min(count, 16) */
   double batched_limit;  /* n * log2(k) bound for the batched launch; < 0 disables it */
   int32_t cluster_size;  /* CTAs per automaton of the cluster launch (1..16); 0 = 8; -1 disables it */
+  double cluster_limit;  /* n * log2(k) bound for the cluster launch, default 160 (above it: worker streams) */
 } sw_batch_tuning;
 
 /* What the last sw_solve_batch on this context did on the device (no

@@ -100,7 +100,11 @@ class _Result(ctypes.Structure):
 
 
 class _BatchTuning(ctypes.Structure):
-    _fields_ = [("workers", ctypes.c_uint32), ("batched_limit", ctypes.c_double), ("cluster_size", ctypes.c_int32)]
+    _fields_ = [("workers", ctypes.c_uint32), ("batched_limit", ctypes.c_double), ("cluster_size", ctypes.c_int32),
+                ("cluster_limit", ctypes.c_double)]
+
+
+DEFAULT_CLUSTER_LIMIT = 160.0  # the library's default (include/synchrowords.h)
 
 
 class _BatchProfile(ctypes.Structure):
@@ -433,7 +437,7 @@ class Context:
                                            res, wc.ctypes.data_as(_U32P), len(wc), lc.ctypes.data_as(f64), len(lc),
                                            reps, ms.ctypes.data_as(f64), ctypes.byref(best)))
         return {"workers": int(best.workers), "batched_limit": float(best.batched_limit),
-                "cluster_size": int(best.cluster_size),
+                "cluster_size": int(best.cluster_size), "cluster_limit": float(best.cluster_limit),
                 "ms": {"workers": {int(w): float(t) for w, t in zip(wc, ms[:len(wc)])},
                        "batched_limit": {float(x): float(t) for x, t in zip(lc, ms[len(wc):])}}}
 
@@ -441,11 +445,13 @@ class Context:
         t = _BatchTuning()
         _check(self._lib.sw_get_batch_tuning(self._h, ctypes.byref(t)))
         return {"workers": int(t.workers), "batched_limit": float(t.batched_limit),
-                "cluster_size": int(t.cluster_size)}
+                "cluster_size": int(t.cluster_size), "cluster_limit": float(t.cluster_limit)}
 
-    def set_batch_tuning(self, workers: int = 0, batched_limit: float = 104.0, cluster_size: int = 0) -> None:
-        """cluster_size: CTAs per automaton of the cluster launch (1..16, 0 = 8, -1 = off)."""
-        t = _BatchTuning(workers, batched_limit, cluster_size)
+    def set_batch_tuning(self, workers: int = 0, batched_limit: float = 104.0, cluster_size: int = 0,
+                         cluster_limit: float = DEFAULT_CLUSTER_LIMIT) -> None:
+        """cluster_size: CTAs per automaton of the cluster launch (1..16, 0 = 8, -1 = off);
+        cluster_limit: the largest n * log2(k) the cluster launch takes."""
+        t = _BatchTuning(workers, batched_limit, cluster_size, cluster_limit)
         _check(self._lib.sw_set_batch_tuning(self._h, ctypes.byref(t)))
 
     def last_batch_profile(self) -> dict:

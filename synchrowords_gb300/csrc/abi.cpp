@@ -41,7 +41,7 @@ struct sw_context {
   std::unique_ptr<sw::Solver> solver;
   std::vector<std::unique_ptr<sw::Solver>> workers;  // extra streams for sw_solve_batch
   SmallBatchState small;
-  sw_batch_tuning tuning{0, 104.0, 0};  // sw_autotune_batch / sw_set_batch_tuning
+  sw_batch_tuning tuning{0, 104.0, 0, 160.0};  // sw_autotune_batch / sw_set_batch_tuning
 };
 
 namespace {
@@ -309,8 +309,8 @@ void start_round(sw_context* ctx, DeviceRound& D, const std::vector<uint32_t> sm
       S.c_tags_used = 0;
     }
     S.c_tags_used += tags;
-    S.c_stats.reserve(sizeof(uint64_t) * 4);
-    SW_CUDA(cudaMemsetAsync(S.c_stats.p, 0, sizeof(uint64_t) * 4, S.stream));
+    S.c_stats.reserve(sizeof(uint64_t) * 9);
+    SW_CUDA(cudaMemsetAsync(S.c_stats.p, 0, sizeof(uint64_t) * 9, S.stream));
   }
   SW_CUDA(cudaMemcpyAsync(S.inst.p, inst.data(), sizeof(sw::SmallInstance) * inst.size(), cudaMemcpyHostToDevice,
                           S.stream));
@@ -352,7 +352,7 @@ std::vector<uint32_t> finish_round(sw_context* ctx, DeviceRound& D, const uint32
   const size_t m = D.order.size();
   std::vector<sw::SmallResult> R(m);
   std::vector<uint8_t> words((size_t)D.word_stride * m);
-  uint64_t cst[4] = {0, 0, 0, 0};
+  uint64_t cst[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   SW_CUDA(cudaMemcpyAsync(R.data(), S.results.p, sizeof(sw::SmallResult) * m, cudaMemcpyDeviceToHost, S.stream));
   SW_CUDA(cudaMemcpyAsync(words.data(), S.words.p, words.size(), cudaMemcpyDeviceToHost, S.stream));
   const bool any_cluster = std::find(D.engine.begin(), D.engine.end(), 1) != D.engine.end();
@@ -426,6 +426,10 @@ std::vector<uint32_t> finish_round(sw_context* ctx, DeviceRound& D, const uint32
                  "[sw] device round: %zu automata in %d launches, %.3f ms; batched launch %zu solved / %zu over "
                  "capacity / %zu unfinished; cluster launch %zu / %zu / %zu\n",
                  m, D.launches, (double)ms, st[0][0], st[0][1], st[0][2], st[1][0], st[1][1], st[1][2]);
+    if (any_cluster)
+      std::fprintf(stderr, "[sw] cluster launch cycles (rank 0, summed over automata): expand %.3g, dedup %.3g, "
+                   "visited insert %.3g, meet %.3g, result %.3g\n", (double)cst[4], (double)cst[5],
+                   (double)cst[6], (double)cst[7], (double)cst[8]);
   }
   return again;
 }
@@ -495,7 +499,7 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
       const bool small_ok = ok && k <= 4 && (double)n * std::log2((double)k) <= ctx->tuning.batched_limit;
       if (small_ok)
         small[(n - 1) / 64].push_back(i);
-      else if (ok && cluster_on)
+      else if (ok && cluster_on && (double)n * std::log2((double)std::max(k, 2u)) <= ctx->tuning.cluster_limit)
         cluster[(n - 1) / 64].push_back(i);
       else
         streamed.push_back(i);

@@ -21,9 +21,9 @@
 //   * the meet check f ⊆ B (f ∩ b' = ∅) stages the backward layer bit-sliced:
 //     for every state q a bitmap over the layer's rows (bit j set when q lies
 //     in B_j), built in shared memory by a ballot transpose.  A warp then takes
-//     one forward set f at a time and ANDs the bitmaps of f's few states, 32
-//     rows per lane-word, stopping as soon as every word is zero; a word still
-//     nonzero when f's states run out names a B_j ⊇ f;
+//     one forward set f at a time and ANDs the bitmaps of f's states, rarest
+//     first, 32 rows per lane-word, stopping as soon as every word is zero; a
+//     word still nonzero when f's states run out names a B_j ⊇ f;
 //   * the word is traced back through per-layer origin records.
 // The search is the one k_small_batch (batch_small.cu) runs, with the same
 // exactness argument: one side grows by one layer per step, every total
@@ -267,6 +267,14 @@ __global__ void __launch_bounds__(kCtThreads, 1)
     u32 cnt0 = 1, cnt1 = sc, used0 = 1, used1 = sc, cur0 = 0, cur1 = 0, depth0 = 0, depth1 = 0;
     u64 my_pairs = 0, my_children = 0, my_staged = 0;
     u32 steps = 0;
+    // cycles between the cluster barriers, per phase (rank 0, thread 0): stats[4..8]
+    long long clk = clock64();
+    u64 ph[5] = {0, 0, 0, 0, 0};
+    auto lap = [&](int i) {
+      const long long t = clock64();
+      ph[i] += (u64)(t - clk);
+      clk = t;
+    };
     for (u32 rt = 0; status == kRunning; ++rt) {
       if (rt >= I.max_len) {
         status = 2;
@@ -325,6 +333,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         __syncwarp();
       }
       cluster_barrier();
+      lap(0);
       const u32 ltag = ld_volatile(&ctl->ltag);
       // ---- duplicates: drop children equal to a visited row or to a sibling ----
       const u32 par = rt & 1u;
@@ -380,6 +389,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
       }
       my_children += c;
       cluster_barrier();
+      lap(1);
       const u32 f = ld_volatile(&ctl->fcount[par]);
       // ---- the kept rows join the side's visited table ----
       for (u32 j = gtid; j < f; j += G) {
@@ -399,6 +409,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         (X ? m_cnt1 : m_cnt0)[depthX + 1] = f;
       }
       cluster_barrier();
+      lap(2);
       if (X) {
         cur1 = usedX;
         used1 = usedX + f;
@@ -483,12 +494,15 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         for (u32 t = 0; fw0 + t < fw1; ++t) {
           u32 acc[4] = {acc0[0], acc0[1], acc0[2], acc0[3]};
           bool alive = true;
+          // rarest states first: states are numbered by decreasing frequency,
+          // so the last state of f (the lowest set bit of its last word) thins
+          // the candidate rows fastest
 #pragma unroll
-          for (int w = 0; w < W; ++w) {
+          for (int w = W - 1; w >= 0; --w) {
             u64 v = __shfl_sync(0xffffffffu, myf[w], t);
             while (v && alive) {
-              const u32 j = __clzll((long long)v);  // state 64 w + j (bit 63 - j)
-              v &= ~(0x8000000000000000ULL >> j);
+              const u32 j = 63 - (__ffsll((long long)v) - 1);  // state 64 w + j (bit 63 - j)
+              v &= v - 1;
               const uint4 col = reinterpret_cast<const uint4*>(s_col + (64 * w + j) * kCtGroups)[lane];
               acc[0] &= col.x;
               acc[1] &= col.y;
@@ -514,6 +528,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         __syncthreads();  // the staged chunk stays until every warp is done with it
       }
       cluster_barrier();
+      lap(3);
       if (ld_volatile(&ctl->found)) {
         status = 0;
         length = rt + 1;
@@ -551,6 +566,8 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         atomicAdd(&stats[0], (unsigned long long)my_pairs);
         atomicAdd(&stats[1], (unsigned long long)my_children);
         atomicAdd(&stats[3], (unsigned long long)steps);
+        lap(4);
+        for (int i = 0; i < 5; ++i) atomicAdd(&stats[4 + i], (unsigned long long)ph[i]);
       }
     }
     if (stats && tid == 0 && my_staged) atomicAdd(&stats[2], (unsigned long long)my_staged);

@@ -47,19 +47,21 @@ def check_against_golden(autos, res):
 def test_autotune_batch_picks_candidates_and_keeps_results(native_lib):
     import synchrowords_gb300 as sw
     ctx = sw.Context(0)  # its own context: the tuning stays with it
-    assert ctx.get_batch_tuning() == {"workers": 0, "batched_limit": 104.0, "cluster_size": 0}
+    assert ctx.get_batch_tuning() == {"workers": 0, "batched_limit": 104.0, "cluster_size": 0,
+                                      "cluster_limit": sw.DEFAULT_CLUSTER_LIMIT}
     autos = gen.batch(GOLD["count"], GOLD["seed"])[:200]
     tuned = ctx.autotune_batch(autos, PLAN, workers=(2, 6), limits=(-1.0, 104.0), reps=1)
     assert tuned["workers"] in (2, 6) and tuned["batched_limit"] in (-1.0, 104.0)
     assert set(tuned["ms"]["workers"]) == {2, 6} and set(tuned["ms"]["batched_limit"]) == {-1.0, 104.0}
     assert all(t > 0 for d in tuned["ms"].values() for t in d.values())
     assert ctx.get_batch_tuning() == {"workers": tuned["workers"], "batched_limit": tuned["batched_limit"],
-                                      "cluster_size": 0}
+                                      "cluster_size": 0,
+                                      "cluster_limit": sw.DEFAULT_CLUSTER_LIMIT}
     check_against_golden(autos, ctx.solve_batch(autos, PLAN))  # workers = 0: the tuned count
     # every route gives the same answers: worker streams only, the shared-memory
     # launch for all it accepts, the cluster launch for all, and clusters of 4 and 16 CTAs
     for limit, cs in ((-1.0, -1), (1024.0, -1), (-1.0, 0), (-1.0, 4), (-1.0, 16)):
-        ctx.set_batch_tuning(workers=4, batched_limit=limit, cluster_size=cs)
+        ctx.set_batch_tuning(workers=4, batched_limit=limit, cluster_size=cs, cluster_limit=1e9)
         check_against_golden(autos, ctx.solve_batch(autos, PLAN))
         prof = ctx.last_batch_profile()
         if cs >= 0:

@@ -246,7 +246,7 @@ def test_c2_n200_cluster_launch_matches_reference(native_lib, cluster):
     want = g["reference"]["exact_default"]["results"]
     autos = [(200, 2, random_dfa(200, 2, s)) for s in g["seeds"]]
     with sw.Context(0) as c:
-        c.set_batch_tuning(workers=16, batched_limit=104.0, cluster_size=cluster)
+        c.set_batch_tuning(workers=16, batched_limit=104.0, cluster_size=cluster, cluster_limit=1e9)
         res = c.solve_batch(autos, EXACT)
         prof = c.last_batch_profile()
     assert prof["cluster_solved"] == 16 and prof["streamed"] == 0, prof
@@ -271,7 +271,7 @@ def test_cluster_launch_random_sizes_against_the_streamed_path(native_lib):
         k = rng.choice([kk for kk in (1, 2, 3, 4, 7, 16) if n * kk <= (4096 if kk <= 2 else 520)])
         autos.append((n, k, random_dfa(n, k, 4000 + i)))
     with sw.Context(0) as c:
-        c.set_batch_tuning(workers=8, batched_limit=-1.0, cluster_size=0)
+        c.set_batch_tuning(workers=8, batched_limit=-1.0, cluster_size=0, cluster_limit=1e9)
         res = c.solve_batch(autos, EXACT)
         prof = c.last_batch_profile()
         c.set_batch_tuning(workers=8, batched_limit=-1.0, cluster_size=-1)
