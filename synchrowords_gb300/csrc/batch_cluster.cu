@@ -18,14 +18,12 @@
 //     layer) and one over the children of the step.  Slots are tagged with a
 //     number unique to the search (visited) or the step (children), so no
 //     table is cleared between automata or steps;
-//   * the meet check f ∩ b' = ∅ (f ⊆ B) re-expresses the reference's trie
-//     pruning as the streamed subset check does: whenever the forward layer
-//     changes it is counting-sorted by its 16 most frequent states (the top 16
-//     bits of word 0) and every 64-row tile and 1024-row super-tile keeps the
-//     AND of its rows.  Chunks of 4096 sorted rows are staged in shared memory
-//     and every thread holds one backward complement b'; a warp skips a range
-//     whose AND meets every lane's b' (then every row of it does) and tests the
-//     rows of the others four at a time, word 0 first;
+//   * the meet check f ⊆ B (f ∩ b' = ∅) stages the backward layer bit-sliced:
+//     for every state q a bitmap over the layer's rows (bit j set when q lies
+//     in B_j), built in shared memory by a ballot transpose.  A warp then takes
+//     one forward set f at a time and ANDs the bitmaps of f's states, rarest
+//     first, 32 rows per lane-word, stopping as soon as every word is zero; a
+//     word still nonzero when f's states run out names a B_j ⊇ f;
 //   * the word is traced back through per-layer origin records.
 // The search is the one k_small_batch (batch_small.cu) runs, with the same
 // exactness argument: one side grows by one layer per step, every total
@@ -49,8 +47,9 @@ namespace {
 constexpr int kCtThreads = 1024;
 constexpr int kCtWarps = kCtThreads / 32;
 constexpr u32 kCtMaxDepth = 1024;   // layers per side
-constexpr u32 kCtChunkRows = 4096;  // sorted forward rows per meet-check chunk (64 tiles, 4 super-tiles)
-constexpr u32 kCtBuckets = 1u << 16;  // counting-sort buckets: states 0..15 of a forward row
+constexpr u32 kCtChunkRows = 4096;  // backward rows per bit-sliced meet-check chunk
+constexpr u32 kCtGroups = kCtChunkRows / 32;  // 32-row bitmap words per state and chunk
+constexpr u32 kCtFSlice = 32 * kCtWarps;  // forward sets per meet-check unit (32 per warp)
 constexpr u32 kCtMaxNK = 4096;      // n * k of the transition table staged per CTA
 constexpr u32 kRunning = 255;
 
@@ -120,7 +119,7 @@ static_assert(sizeof(ClusterCtl) == 256, "control block is one 256-byte line");
 // any width and any cluster count finds every table slot either zero or holding
 // a tag an earlier search took, never row data of another layout read as a tag.
 struct ClusterRegion {
-  size_t vtab[2], ltab, meta, vis[2], org[2], ch, hist, fs, fperm, tmask, smask, bytes;
+  size_t vtab[2], ltab, meta, vis[2], org[2], ch, bytes;
 };
 
 template <int W>
@@ -141,13 +140,6 @@ __host__ __device__ inline ClusterRegion cluster_region(const ClusterCaps& c) {
   r.org[0] = take(sizeof(u32) * (size_t)c.vis);
   r.org[1] = take(sizeof(u32) * (size_t)c.vis);
   r.ch = take(sizeof(u64) * W * (size_t)c.ch);
-  // the forward layer sorted for the meet check (a layer is at most one
-  // step's children), its tile and super-tile masks
-  r.hist = take(sizeof(u32) * kCtBuckets);
-  r.fs = take(sizeof(u64) * W * (size_t)c.ch);
-  r.fperm = take(sizeof(u32) * (size_t)c.ch);
-  r.tmask = take(sizeof(u64) * W * ((size_t)c.ch / 64 + 1));
-  r.smask = take(sizeof(u64) * W * ((size_t)c.ch / 1024 + 1));
   r.bytes = o;
   return r;
 }
@@ -163,14 +155,13 @@ __global__ void __launch_bounds__(kCtThreads, 1)
     k_cluster_batch(const SmallInstance* __restrict__ inst, u32 count, const uint8_t* __restrict__ delta_pool,
                     const uint8_t* __restrict__ seed_pool, SmallResult* results, uint8_t* words, u32 word_stride,
                     uint8_t* scratch, size_t region_stride, ClusterCaps caps, u32* counter, u64* stats) {
-  extern __shared__ __align__(16) u64 s_stage[];  // a chunk of sorted forward rows, then its tile and super-tile masks
+  extern __shared__ __align__(16) u32 s_col[];   // bitmaps: s_col[q * kCtGroups + g], q < 64 W
   __shared__ uint8_t s_delta[kCtMaxNK];          // delta[q * k + a]
   __shared__ uint8_t s_isrc[kCtMaxNK];           // preimage lists, letter-major CSR
   __shared__ u32 s_ibeg[kCtMaxNK + 16 + 1];      // list of (a, t): [s_ibeg[a*(n+1)+t], s_ibeg[a*(n+1)+t+1])
   __shared__ u32 s_fill[kCtMaxNK];
   __shared__ u64 s_par[kCtWarps][W];
   __shared__ u32 s_flag;
-  __shared__ u32 s_wsum[kCtWarps];
 
   const u32 rank = cluster_rank(), CS = cluster_ctas();
   const u32 tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -194,11 +185,6 @@ __global__ void __launch_bounds__(kCtThreads, 1)
   u64* const vt0 = reinterpret_cast<u64*>(base + R.vtab[0]);
   u64* const vt1 = reinterpret_cast<u64*>(base + R.vtab[1]);
   u64* const lt = reinterpret_cast<u64*>(base + R.ltab);
-  u32* const hist = reinterpret_cast<u32*>(base + R.hist);
-  u64* const Fs = reinterpret_cast<u64*>(base + R.fs);
-  u32* const Fperm = reinterpret_cast<u32*>(base + R.fperm);
-  u64* const tmask = reinterpret_cast<u64*>(base + R.tmask);
-  u64* const smask = reinterpret_cast<u64*>(base + R.smask);
   const u32 vmask = (1u << caps.vtab_bits) - 1, lmask = (1u << caps.ltab_bits) - 1;
 
   for (;;) {
@@ -280,7 +266,7 @@ __global__ void __launch_bounds__(kCtThreads, 1)
     // per-side counters, identical in every thread of the cluster
     u32 cnt0 = 1, cnt1 = sc, used0 = 1, used1 = sc, cur0 = 0, cur1 = 0, depth0 = 0, depth1 = 0;
     u64 my_pairs = 0, my_children = 0, my_staged = 0;
-    u32 steps = 0, sorted_depth = 0xffffffffu;  // depth of the forward layer held sorted in Fs
+    u32 steps = 0;
     // cycles between the cluster barriers, per phase (rank 0, thread 0): stats[4..8]
     long long clk = clock64();
     u64 ph[5] = {0, 0, 0, 0, 0};
@@ -445,146 +431,99 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         status = 2;
         break;
       }
-      // ---- meet check of the current layers: some f ∩ b'_j = ∅ (f ⊆ B_j) ----
+      // ---- meet check of the current layers: some f ⊆ B_j (f ∩ b'_j = ∅) ----
       const u32 nF = cnt0, nB = cnt1;
-      if (sorted_depth != depth0) {
-        // the forward layer changed: counting sort of its rows by states
-        // 0..15 (the top 16 bits of word 0, the most frequent image states)
-        // into Fs, with each sorted row's layer index in Fperm, then the AND
-        // of every 64-row tile and 1024-row super-tile
-        const u64* Frows = V0 + (size_t)cur0 * W;
-        for (u32 b = gtid; b < kCtBuckets; b += G) hist[b] = 0;
-        cluster_barrier();
-        for (u32 r = gtid; r < nF; r += G) atomicAdd(&hist[(u32)(Frows[(size_t)r * W] >> 48)], 1u);
-        cluster_barrier();
-        if (rank == 0) {  // exclusive prefix over the buckets, 64 per thread
-          constexpr u32 per = kCtBuckets / kCtThreads;
-          u32 sum = 0;
-          for (u32 b = 0; b < per; ++b) sum += hist[tid * per + b];
-          u32 x = sum;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const u32 y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= (u32)o) x += y;
-          }
-          if (lane == 31) s_wsum[warp] = x;
-          __syncthreads();
-          if (warp == 0) {
-            u32 v = s_wsum[lane], inc = v;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-              const u32 y = __shfl_up_sync(0xffffffffu, inc, o);
-              if (lane >= (u32)o) inc += y;
-            }
-            s_wsum[lane] = inc - v;
-          }
-          __syncthreads();
-          u32 run = s_wsum[warp] + x - sum;
-          for (u32 b = 0; b < per; ++b) {
-            const u32 h = hist[tid * per + b];
-            hist[tid * per + b] = run;
-            run += h;
-          }
-        }
-        cluster_barrier();
-        for (u32 r = gtid; r < nF; r += G) {
-          const u32 pos = atomicAdd(&hist[(u32)(Frows[(size_t)r * W] >> 48)], 1u);
-#pragma unroll
-          for (int w = 0; w < W; ++w) Fs[(size_t)pos * W + w] = Frows[(size_t)r * W + w];
-          Fperm[pos] = r;
-        }
-        cluster_barrier();
-        const u32 tiles = (nF + 63) / 64, supers = (nF + 1023) / 1024;
-        for (u32 t = gwarp; t < tiles + supers; t += NW) {  // warp per tile, then per super-tile
-          const bool sup = t >= tiles;
-          const u32 r0 = sup ? (t - tiles) * 1024 : t * 64;
-          const u32 nr = sup ? 1024u : 64u;
-#pragma unroll
-          for (int w = 0; w < W; ++w) {
-            u64 a = ~0ULL;
-            for (u32 r = r0 + lane; r < min(nF, r0 + nr); r += 32) a &= Fs[(size_t)r * W + w];
-#pragma unroll
-            for (int o = 16; o; o >>= 1) a &= __shfl_xor_sync(0xffffffffu, a, o);
-            if (lane == 0) (sup ? smask + (size_t)(t - tiles) * W : tmask + (size_t)t * W)[w] = a;
-          }
-        }
-        cluster_barrier();
-        sorted_depth = depth0;
-      }
-      // units: (chunk of 4096 sorted forward rows) x (block of 1024 backward
-      // complements, one per thread).  A warp skips a super-tile or tile whose
-      // AND meets every lane's b' (every row of it then meets b'), and tests
-      // the rows of the others four at a time, word 0 first.
-      const u64* Brows = V1 + (size_t)cur1 * W;
-      const u32 chunks = (nF + kCtChunkRows - 1) / kCtChunkRows;
-      const u32 qblocks = (nB + kCtThreads - 1) / kCtThreads;
-      const u32 units = chunks * qblocks;
+      const u64* Frows = V0 + (size_t)cur0 * W;
+      const u64* Brows = V1 + (size_t)cur1 * W;  // complements b' = Q \ B
+      const u32 chunks = (nB + kCtChunkRows - 1) / kCtChunkRows;
+      const u32 fslices = (nF + kCtFSlice - 1) / kCtFSlice;
+      const u32 units = chunks * fslices;
       my_pairs += (u64)nF * nB;
       u32 staged = 0xffffffffu;
-      u64* const s_rows = s_stage;
-      u64* const s_tm = s_stage + (size_t)kCtChunkRows * W;
-      u64* const s_sm = s_tm + (size_t)(kCtChunkRows / 64) * W;
       for (u32 u = rank; u < units; u += CS) {
         if (tid == 0) s_flag = ld_volatile(&ctl->found);
         __syncthreads();
         if (s_flag != 0) break;  // block-uniform
-        const u32 chunk = u / qblocks, qb = u - chunk * qblocks;
+        const u32 chunk = u / fslices, fs = u - chunk * fslices;
         const u32 r0 = chunk * kCtChunkRows;
-        const u32 rows = min(kCtChunkRows, nF - r0);
-        const u32 ntile = (rows + 63) / 64, nsup = (rows + 1023) / 1024;
+        const u32 rows = min(kCtChunkRows, nB - r0);
+        const u32 groups = (rows + 31) / 32;
         if (chunk != staged) {
-          for (u32 x = tid; x < rows * W; x += kCtThreads) s_rows[x] = Fs[(size_t)r0 * W + x];
-          for (u32 x = tid; x < ntile * W; x += kCtThreads) s_tm[x] = tmask[(size_t)(r0 / 64) * W + x];
-          for (u32 x = tid; x < nsup * W; x += kCtThreads) s_sm[x] = smask[(size_t)(r0 / 1024) * W + x];
+          // transpose: bit j of s_col[q * kCtGroups + g] says state q lies in
+          // B_{r0 + 32 g + j}; warp per 32-row group, one ballot per state
+          for (u32 g = warp; g < groups; g += kCtWarps) {
+            const u32 r = 32 * g + lane;
+            u64 b[W];
+#pragma unroll
+            for (int w = 0; w < W; ++w)
+              b[w] = r < rows ? ~Brows[(size_t)(r0 + r) * W + w] & valid_mask((int)n, w) : 0ULL;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+              u32 keep0 = 0, keep1 = 0;
+#pragma unroll 8
+              for (int j = 0; j < 64; ++j) {
+                const u32 col = __ballot_sync(0xffffffffu, (b[w] >> (63 - j)) & 1ULL);
+                if (lane == (u32)(j & 31)) {
+                  if (j < 32) keep0 = col;
+                  else keep1 = col;
+                }
+              }
+              s_col[(64 * w + lane) * kCtGroups + g] = keep0;
+              s_col[(64 * w + 32 + lane) * kCtGroups + g] = keep1;
+            }
+          }
           staged = chunk;
           my_staged += (u64)rows * W * 8;
           __syncthreads();
         }
-        const u32 qi = qb * kCtThreads + tid;
-        const bool valid = qi < nB;
-        u64 q[W];
+        // warp per 32 forward sets: lane l fetches set f0 + 32 warp + l, then
+        // the warp takes them one by one (broadcast by shuffle) and ANDs the
+        // bitmaps of each set's states; lane l owns the chunk's 32-row words
+        // 4l .. 4l + 3 (one 16-byte shared load per state)
+        const u32 fw0 = fs * kCtFSlice + warp * 32;
+        const u32 fw1 = min(nF, fw0 + 32);
+        u64 myf[W];
 #pragma unroll
-        for (int w = 0; w < W; ++w) q[w] = valid ? Brows[(size_t)qi * W + w] : ~0ULL;
-        u32 hit = 0xffffffffu;
-        for (u32 sp = 0; sp < nsup; ++sp) {
-          bool need_s = valid && hit == 0xffffffffu;
+        for (int w = 0; w < W; ++w) myf[w] = fw0 + lane < fw1 ? Frows[(size_t)(fw0 + lane) * W + w] : 0ULL;
+        u32 acc0[4];
 #pragma unroll
-          for (int w = 0; w < W; ++w) need_s = need_s && !(s_sm[sp * W + w] & q[w]);
-          if (!__any_sync(0xffffffffu, need_s)) continue;
-          const u32 t1 = min(ntile, sp * 16 + 16);
-          for (u32 t = sp * 16; t < t1; ++t) {
-            bool need = need_s && hit == 0xffffffffu;
+        for (int i = 0; i < 4; ++i) {
+          const u32 g = 4 * lane + i;
+          acc0[i] = g < groups ? (32 * g + 32 <= rows ? 0xffffffffu : (1u << (rows - 32 * g)) - 1u) : 0u;
+        }
+        for (u32 t = 0; fw0 + t < fw1; ++t) {
+          u32 acc[4] = {acc0[0], acc0[1], acc0[2], acc0[3]};
+          bool alive = true;
+          // rarest states first: states are numbered by decreasing frequency,
+          // so the last state of f (the lowest set bit of its last word) thins
+          // the candidate rows fastest
 #pragma unroll
-            for (int w = 0; w < W; ++w) need = need && !(s_tm[t * W + w] & q[w]);
-            if (!__any_sync(0xffffffffu, need)) continue;
-            if (need) {
-              const u32 tr = min(64u, rows - t * 64);
-              const u64* tb = s_rows + (size_t)t * 64 * W;
-              for (u32 r = 0; r < tr && hit == 0xffffffffu; r += 4) {
-                u32 pass = 0;
-#pragma unroll
-                for (int jj = 0; jj < 4; ++jj)
-                  if (r + jj < tr && !(tb[(size_t)(r + jj) * W] & q[0])) pass |= 1u << jj;
-                if (!pass) continue;
-#pragma unroll
-                for (int jj = 0; jj < 4; ++jj) {
-                  if (!((pass >> jj) & 1u)) continue;
-                  const u64* fr = tb + (size_t)(r + jj) * W;
-                  bool dis = true;
-#pragma unroll
-                  for (int w = 1; w < W; ++w) dis = dis && !(fr[w] & q[w]);
-                  if (dis) {
-                    hit = t * 64 + r + jj;
-                    break;
-                  }
-                }
-              }
+          for (int w = W - 1; w >= 0; --w) {
+            u64 v = __shfl_sync(0xffffffffu, myf[w], t);
+            while (v && alive) {
+              const u32 j = 63 - (__ffsll((long long)v) - 1);  // state 64 w + j (bit 63 - j)
+              v &= v - 1;
+              const uint4 col = reinterpret_cast<const uint4*>(s_col + (64 * w + j) * kCtGroups)[lane];
+              acc[0] &= col.x;
+              acc[1] &= col.y;
+              acc[2] &= col.z;
+              acc[3] &= col.w;
+              alive = __any_sync(0xffffffffu, (acc[0] | acc[1] | acc[2] | acc[3]) != 0u);
             }
           }
-        }
-        if (hit != 0xffffffffu && atomicCAS(&ctl->found, 0u, 1u) == 0u) {
-          ctl->fi = Fperm[r0 + hit];
-          ctl->bj = qi;
+          if (alive) {  // some B_j contains every state of f
+            u32 hit = 0xffffffffu;
+#pragma unroll
+            for (int i = 3; i >= 0; --i)
+              if (acc[i]) hit = 32 * (4 * lane + i) + __ffs(acc[i]) - 1;
+            const u32 who = __ballot_sync(0xffffffffu, hit != 0xffffffffu);
+            const u32 bj = __shfl_sync(0xffffffffu, hit, __ffs(who) - 1);
+            if (lane == 0 && atomicCAS(&ctl->found, 0u, 1u) == 0u) {
+              ctl->fi = fw0 + t;
+              ctl->bj = r0 + bj;
+            }
+            break;
+          }
         }
         __syncthreads();  // the staged chunk stays until every warp is done with it
       }
@@ -649,8 +588,8 @@ const void* cluster_fn_w(int W) {
   }
   throw std::runtime_error("cluster batch: unsupported width");
 }
-// a chunk of sorted forward rows and its 64 tile and 4 super-tile masks
-size_t col_smem(int W) { return sizeof(u64) * (size_t)W * (kCtChunkRows + kCtChunkRows / 64 + kCtChunkRows / 1024); }
+// bitmaps of 64 W states x kCtGroups words
+size_t col_smem(int W) { return sizeof(u32) * 64 * (size_t)W * kCtGroups; }
 
 std::mutex g_cluster_mu;
 
