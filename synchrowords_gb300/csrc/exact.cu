@@ -69,6 +69,7 @@ class Engine {
     SW_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
     pinned.reserve(4096);
     SW_CUDA(cudaMalloc(&d_misc, 64 * sizeof(u32)));
+    SW_CUDA(cudaMemset(d_misc, 0, 64 * sizeof(u32)));
     mlp = std::make_unique<MlpRunner>(stream);
   }
   ~Engine() {
@@ -142,7 +143,13 @@ class Engine {
     }
     prof_on = false;
   }
-  u32* d_misc = nullptr;  // [0..3] witness, [8] scan total
+  u32* d_misc = nullptr;  // [0..3] witness, [8] scan total, [kScanErrWord] subset-scan copy timeout
+  static constexpr int kScanErrWord = 60;
+  // Throws if a subset-check launch reported a tile copy that never arrived
+  // (its bounded wait ran out); `w` is the pinned copy of d_misc[kScanErrWord].
+  static void check_scan_error(u32 w) {
+    if (w) throw CudaError("subset check: a tile copy did not complete within its wait limit");
+  }
   // tables
   DevBuf t_delta, t_beg, t_src;
   TransTables tables;
@@ -230,7 +237,7 @@ class Engine {
     // algorithmic bytes: the query rows plus every S tile staged on chip
     timed(0, (double)q * 8.0 * W, [&] {
       launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, stream,
-                          prof_on ? d_query_bytes : nullptr);
+                          prof_on ? d_query_bytes : nullptr, d_misc + kScanErrWord);
     });
     count_launch(2);
     if (st) {
@@ -483,8 +490,10 @@ class Engine {
     query(W, kQueryDisjoint, F.rows.as<u64>(), F.count, Q, q, n, nullptr, true);
     if (st) st->meet_pairs += (u64)F.count * q;
     SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaMemcpyAsync(pinned.as<u32>() + 4, d_misc + kScanErrWord, sizeof(u32), cudaMemcpyDeviceToHost, stream));
     SW_CUDA(cudaStreamSynchronize(stream));
     const u32* w = pinned.as<u32>();
+    check_scan_error(w[4]);
     if (!w[0]) return false;
     *qi = w[1];
     *si = w[2];
@@ -772,9 +781,12 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
             n, nullptr, true);
     st.meet_pairs += (u64)E.F.count * E.B.count;
     SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaMemcpyAsync(E.pinned.as<u32>() + 4, E.d_misc + Engine::kScanErrWord, sizeof(u32),
+                            cudaMemcpyDeviceToHost, E.stream));
     SW_CUDA(cudaStreamSynchronize(E.stream));
     const auto t_end = std::chrono::steady_clock::now();
     const u32* w = E.pinned.as<u32>();
+    Engine::check_scan_error(w[4]);
     t_iter_last = std::chrono::duration<double>(t_end - t_iter0).count();
     if (E.B.count)
       t_meet_per_query = std::chrono::duration<double>(t_end - t_meet_host0).count() / (double)E.B.count;
@@ -1076,8 +1088,11 @@ void Solver::subsets_check(uint32_t n, const uint64_t* sets, uint64_t set_count,
   E.query(W, proper ? kQueryProperSubset : kQuerySubset, E.keys.as<u64>(), u,
           E.ch_rows.as<u64>(), q, (int)n, E.flags_b.as<u32>(), false);
   std::vector<u32> flags(q);
+  u32 scan_err = 0;
   SW_CUDA(cudaMemcpyAsync(flags.data(), E.flags_b.p, sizeof(u32) * q, cudaMemcpyDeviceToHost, E.stream));
+  SW_CUDA(cudaMemcpyAsync(&scan_err, E.d_misc + Engine::kScanErrWord, sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
   SW_CUDA(cudaStreamSynchronize(E.stream));
+  Engine::check_scan_error(scan_err);
   for (u32 i = 0; i < q; ++i) results[i] = flags[i] ? 1 : 0;
 }
 

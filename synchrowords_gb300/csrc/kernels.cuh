@@ -75,11 +75,13 @@ enum QueryMode : int {
 // index).  S is cut into 64-row tiles; tile_and[t] (W words) = AND of the
 // tile's rows, from launch_tile_and.  `flags` must start zeroed (non-stop
 // mode).  `bytes_ctr` (optional) accumulates the bytes of S tiles staged on
-// chip.
+// chip.  S must start 16-byte aligned (its tiles move by bulk copies).  *err
+// is set to 1 when a wait for a tile copy runs out (its bounded poll limit);
+// the results of that launch are then incomplete.
 size_t subset_check_temp_bytes(int W, u32 m);
 void launch_tile_and(int W, const u64* S, u32 m, u64* tile_and, cudaStream_t s);
 void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* tile_and, const u64* Q, u32 q, int n,
-                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr = nullptr);
+                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr, u32* err);
 
 // out = sorted merge of two sorted, mutually disjoint row arrays.
 void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);

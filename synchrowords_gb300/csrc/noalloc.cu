@@ -30,11 +30,11 @@ namespace sw {
 namespace {
 
 // masks for SW_NOALLOC_MAX_SETS rows of 8 words: one per 64-row tile plus one
-// per 1024-row super-tile (see subset_check.cu), plus 4 words for the unused
-// meet-mode witness
+// per 1024-row super-tile (see subset_check.cu), plus 4 words: three for the
+// unused meet-mode witness, one for the kernel's copy-timeout word
 constexpr size_t kMaxTiles = (SW_NOALLOC_MAX_SETS + 63) / 64;
 constexpr size_t kMaxSupers = (SW_NOALLOC_MAX_SETS + 1023) / 1024;
-constexpr size_t kScratchWords = (kMaxTiles + kMaxSupers) * 8 + 4;
+constexpr size_t kScratchWords = (kMaxTiles + kMaxSupers) * 8 + 4;  // + witness, error word
 
 __device__ __align__(256) unsigned long long g_noalloc_scratch[kScratchWords];
 
@@ -131,7 +131,7 @@ extern "C" int sw_subsets_check_device_noalloc(uint32_t n, const uint64_t* d_set
     launch_tile_and(W, reinterpret_cast<const u64*>(d_sets), (u32)set_count, masks, s);
     launch_subset_check(W, proper ? kQueryProperSubset : kQuerySubset, reinterpret_cast<const u64*>(d_sets),
                         (u32)set_count, masks, reinterpret_cast<const u64*>(d_checks), (u32)check_count, (int)n,
-                        d_results, witness, false, s, nullptr);
+                        d_results, witness, false, s, nullptr, witness + 3);
   } catch (const std::exception& ex) {
     g_err = ex.what();
     return SW_ERR_CUDA;

@@ -14,9 +14,10 @@
 //     range.
 // One warp owns 32 consecutive (hence similar) queries and streams the
 // super-tiles of its chunk of S: a range is skipped unless some lane still
-// needs it (__any_sync), a needed tile is staged into the warp's slice of
-// shared memory with one coalesced read, and every lane tests its own query
-// against the staged rows with an early exit on word 0.  No block-wide
+// needs it (__any_sync).  Needed tiles move into the warp's two shared-memory
+// buffers by 1-D bulk copies (cp.async.bulk, completion on one mbarrier per
+// buffer): while the lanes test their queries against one tile, with an
+// early exit on word 0, the next needed tile is already on its way.  No block-wide
 // barriers: warps of a block proceed independently.  Warps stop as soon as all
 // their queries are decided; in meet mode the first hit stops the grid.
 #include <cuda_runtime.h>
@@ -65,13 +66,46 @@ __global__ void k_range_and(const u64* __restrict__ S, u32 m, u64* __restrict__ 
   }
 }
 
+// ---- bulk-copy staging: per-warp double buffer, one mbarrier per buffer ----
+__device__ __forceinline__ u32 smem_addr(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(u64* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+}
+// One 1-D bulk copy global -> shared (16-byte aligned ends, size a multiple
+// of 16) that completes the transaction count of `bar`; issued by one lane.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, u32 bytes, u64* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+// Waits for phase `parity` of `bar` to complete, at most kWaitLimit polls;
+// false when the limit ran out.
+constexpr u32 kWaitLimit = 1u << 24;
+__device__ __forceinline__ bool mbar_wait(u64* bar, u32 parity) {
+  for (u32 it = 0; it < kWaitLimit; ++it) {
+    u32 ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 template <int W, int MODE>
 __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restrict__ S, u32 m,
                                                              const u64* __restrict__ masks, u32 tiles_per_chunk,
                                                              const u64* __restrict__ Q, u32 q, int n,
                                                              u32* __restrict__ flags, u32* witness, int stop,
-                                                             u64* __restrict__ bytes_ctr) {
-  __shared__ __align__(16) u64 s_rows[kWarps][kTileRows * W];
+                                                             u64* __restrict__ bytes_ctr, u32* err) {
+  // per warp: two tile buffers of 64 rows, filled by bulk copies
+  extern __shared__ __align__(128) u64 s_tiles[];  // [kWarps][2][kTileRows * W]
+  __shared__ __align__(8) u64 s_bar[kWarps][2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const u32 qi = (blockIdx.x * kWarps + warp) * 32 + lane;
   const bool valid = qi < q;
@@ -88,53 +122,87 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
   const u32 tiles = n_tiles(m);
   const u64* tile_and = masks;
   const u64* super_and = masks + (size_t)tiles * W;
-  u64* my_rows = s_rows[warp];
+  // buffer b of this warp; bit b of par = phase parity its next copy completes
+  u64* const buf0 = s_tiles + (size_t)(warp * 2) * kTileRows * W;
+  auto buf = [&](int b) { return buf0 + (size_t)b * kTileRows * W; };
+  u64* const bar0 = &s_bar[warp][0];
+  if (lane == 0) {
+    mbar_init(&s_bar[warp][0]);
+    mbar_init(&s_bar[warp][1]);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncwarp();
+  u32 par = 0;
   const u32 t0 = blockIdx.y * tiles_per_chunk;
   const u32 t1 = min(tiles, t0 + tiles_per_chunk);
-  bool need_s = false;
-  for (u32 t = t0; t < t1; ++t) {
-    if (t == t0 || t % kTilesPerSuper == 0) {
-      // entering a super-tile: stop checks, then its mask decides for all
-      // of its tiles in this chunk
-      if (__all_sync(kFullMask, done)) break;
-      if (stop) {
-        u32 f = lane == 0 ? *(volatile u32*)witness : 0u;
-        if (__shfl_sync(kFullMask, f, 0)) break;
+  // next tile >= from that some lane still needs (the AND of every range it
+  // lies in is inside the lane's query), or t1
+  auto advance = [&](u32 from) -> u32 {
+    bool need_s = false;
+    for (u32 t = from; t < t1; ++t) {
+      if (t == from || t % kTilesPerSuper == 0) {
+        const u32 sp = t / kTilesPerSuper;
+        need_s = !done;
+#pragma unroll
+        for (int w = 0; w < W; ++w)
+          if (super_and[(size_t)sp * W + w] & ~c[w]) need_s = false;
+        if (!__any_sync(kFullMask, need_s)) {
+          t = min(t1, (sp + 1) * kTilesPerSuper) - 1;  // skip the rest of this super-tile
+          continue;
+        }
       }
-      const u32 sp = t / kTilesPerSuper;
-      need_s = !done;
+      bool need = need_s && !done;
 #pragma unroll
       for (int w = 0; w < W; ++w)
-        if (super_and[(size_t)sp * W + w] & ~c[w]) need_s = false;
-      if (!__any_sync(kFullMask, need_s)) {
-        t = min(t1, (sp + 1) * kTilesPerSuper) - 1;  // skip the rest of this super-tile
-        continue;
-      }
+        if (tile_and[(size_t)t * W + w] & ~c[w]) need = false;
+      if (__any_sync(kFullMask, need)) return t;
     }
-    bool need = need_s && !done;
+    return t1;
+  };
+  // full tiles move as one bulk copy; the last, partial tile of S with plain loads
+  auto full_tile = [&](u32 t) { return (t + 1) * (u32)kTileRows <= m; };
+  auto issue = [&](u32 t, int b) {
+    if (!full_tile(t)) return;
+    if (lane == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the buffer come first
+      bulk_load(buf(b), S + (size_t)t * kTileRows * W, (u32)(kTileRows * W * 8), bar0 + b);
+    }
+  };
+  bool failed = false;
+  auto land = [&](u32 t, int b) {  // the tile's rows are in buf[b] after this
+    if (full_tile(t)) {
+      if (!mbar_wait(bar0 + b, (par >> b) & 1u)) failed = true;
+      par ^= 1u << b;
+      failed = __any_sync(kFullMask, failed);
+    } else {
+      const u32 r0 = t * kTileRows, rows = m - r0;
+      u64* const d = buf(b);
+      for (u32 i = lane; i < rows * W; i += 32) d[i] = S[(size_t)r0 * W + i];
+      // rows past the end of S never pass the word-0 test below
+      for (u32 i = rows * W + lane; i < (u32)kTileRows * W; i += 32) d[i] = ~0ULL;
+      __syncwarp();
+    }
+  };
+  u32 cur = advance(t0);
+  int b = 0;
+  if (cur < t1) issue(cur, 0);
+  u32 last_super = 0xffffffffu;
+  while (cur < t1) {
+    const u32 nxt = advance(cur + 1);
+    if (nxt < t1) issue(nxt, b ^ 1);  // overlaps with the tests of `cur`
+    land(cur, b);
+    if (failed) {
+      if (lane == 0) atomicExch(err, 1u);
+      if (nxt < t1 && full_tile(nxt)) mbar_wait(bar0 + (b ^ 1), (par >> (b ^ 1)) & 1u);  // bounded
+      return;
+    }
+    const u32 rows = min((u32)kTileRows, m - cur * kTileRows);
+    loaded += rows;
+    bool need = !done;
 #pragma unroll
     for (int w = 0; w < W; ++w)
-      if (tile_and[(size_t)t * W + w] & ~c[w]) need = false;
-    if (!__any_sync(kFullMask, need)) continue;
-    const u32 r0 = t * kTileRows;
-    const u32 rows = min((u32)kTileRows, m - r0);
-    const u64* src = S + (size_t)r0 * W;
-    if (W >= 2) {
-      // 16-byte moves (tile starts are 16-byte aligned: 64 rows of 8W bytes);
-      // an odd word count leaves one word for a plain load
-      const uint4* s4 = reinterpret_cast<const uint4*>(src);
-      uint4* d4 = reinterpret_cast<uint4*>(my_rows);
-      const u32 words = rows * W;
-      for (u32 i = lane; i < words / 2; i += 32) d4[i] = s4[i];
-      if ((words & 1u) && lane == 0) my_rows[words - 1] = src[words - 1];
-    } else {
-      for (u32 i = lane; i < rows; i += 32) my_rows[i] = src[i];
-    }
-    // rows past the end of S never pass the word-0 test below
-    if (rows < (u32)kTileRows)
-      for (u32 i = rows * W + lane; i < (u32)kTileRows * W; i += 32) my_rows[i] = ~0ULL;
-    loaded += rows;
-    __syncwarp();
+      if (tile_and[(size_t)cur * W + w] & ~c[w]) need = false;
+    const u64* my_rows = buf(b);
     if (need) {
       const u64 nc0 = ~c[0];
       // four rows per iteration: independent word-0 tests, full test only
@@ -158,13 +226,13 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
           if (sub && (MODE != kQueryProperSubset || !eq)) {
             hit = true;
             done = true;
-            hit_idx = r0 + r + j;
+            hit_idx = cur * kTileRows + r + j;
             break;
           }
         }
       }
     }
-    __syncwarp();
+    __syncwarp();  // every lane is done with buffer b before it is refilled
     if (stop && hit) {
       if (atomicCAS(witness, 0u, 1u) == 0u) {
         witness[1] = qi;
@@ -172,6 +240,22 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
       }
       hit = false;  // recorded
     }
+    // leave when every lane is decided or, in meet mode, once any warp met
+    bool leave = __all_sync(kFullMask, done);
+    const u32 sp = nxt / kTilesPerSuper;
+    if (!leave && stop && nxt < t1 && sp != last_super) {
+      last_super = sp;
+      u32 f = lane == 0 ? *(volatile u32*)witness : 0u;
+      leave = __shfl_sync(kFullMask, f, 0) != 0;
+    }
+    if (leave) {
+      if (nxt < t1 && full_tile(nxt)) {  // its copy is in flight: wait (bounded) before the buffer goes away
+        if (!mbar_wait(bar0 + (b ^ 1), (par >> (b ^ 1)) & 1u) && lane == 0) atomicExch(err, 1u);
+      }
+      break;
+    }
+    cur = nxt;
+    b ^= 1;
   }
   if (bytes_ctr && lane == 0 && loaded) atomicAdd(bytes_ctr, loaded * 8ULL * W);
   if (hit && !stop) flags[qi] = 1u;
@@ -201,8 +285,9 @@ void launch_tile_and(int W, const u64* S, u32 m, u64* masks, cudaStream_t s) {
 }
 
 void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks, const u64* Q, u32 q, int n,
-                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr) {
+                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr, u32* err) {
   if (!m || !q) return;
+  if (!err) throw std::invalid_argument("subset check: an error word is required");
   const u32 tiles = n_tiles(m);
   const u32 qblocks = (q + kWarps * 32 - 1) / (kWarps * 32);
   // split S into chunks of tiles so that the grid covers the GPU ~16x: per-warp
@@ -216,17 +301,18 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
   const u32 per = (tiles + chunks - 1) / chunks;
   chunks = (tiles + per - 1) / per;
   dim3 grid(qblocks, chunks);
-#define SW_SC(WW)                                                                                              \
-  case WW:                                                                                                     \
-    if (mode == kQuerySubset)                                                                                  \
-      k_subset_scan<WW, kQuerySubset><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags, witness, \
-                                                                   stop, bytes_ctr);                           \
-    else if (mode == kQueryProperSubset)                                                                       \
-      k_subset_scan<WW, kQueryProperSubset><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags,    \
-                                                                         witness, stop, bytes_ctr);            \
-    else                                                                                                       \
-      k_subset_scan<WW, kQueryDisjoint><<<grid, kWarps * 32, 0, s>>>(S, m, masks, per, Q, q, n, flags,        \
-                                                                     witness, stop, bytes_ctr);                \
+  const size_t smem = sizeof(u64) * (size_t)W * kTileRows * 2 * kWarps;  // two tiles per warp
+#define SW_SC_ONE(WW, MM)                                                                                     \
+  {                                                                                                           \
+    if (smem > 48 * 1024) ensure_smem_limit((const void*)k_subset_scan<WW, MM>, (int)smem);                \
+    k_subset_scan<WW, MM><<<grid, kWarps * 32, smem, s>>>(S, m, masks, per, Q, q, n, flags, witness, stop, \
+                                                          bytes_ctr, err);                                   \
+  }
+#define SW_SC(WW)                                                   \
+  case WW:                                                          \
+    if (mode == kQuerySubset) SW_SC_ONE(WW, kQuerySubset)           \
+    else if (mode == kQueryProperSubset) SW_SC_ONE(WW, kQueryProperSubset) \
+    else SW_SC_ONE(WW, kQueryDisjoint)                              \
     break;
   switch (W) {
     SW_SC(1)
@@ -241,6 +327,7 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
       throw std::runtime_error("subset check: unsupported width");
   }
 #undef SW_SC
+#undef SW_SC_ONE
   SW_LAUNCH_CHECK();
 }
 
