@@ -304,7 +304,7 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
   const size_t smem = sizeof(u64) * (size_t)W * kTileRows * 2 * kWarps;  // two tiles per warp
 #define SW_SC_ONE(WW, MM)                                                                                     \
   {                                                                                                           \
-    if (smem > 48 * 1024) ensure_smem_limit((const void*)k_subset_scan<WW, MM>, (int)smem);                \
+    if (smem >= 32 * 1024) ensure_smem_limit((const void*)k_subset_scan<WW, MM>, (int)smem);               \
     k_subset_scan<WW, MM><<<grid, kWarps * 32, smem, s>>>(S, m, masks, per, Q, q, n, flags, witness, stop, \
                                                           bytes_ctr, err);                                   \
   }
