@@ -9,7 +9,10 @@ The reference has no public benchmark suite; these seeded synthetic automata
 stand in with the shapes its configs name.
 
 Printed JSON line (rank 0):
-  value     ms per DFA from CUDA events on the library's stream (max over ranks)
+  value     ms per DFA: the step's time between device-wide synchronisations
+            (the step runs on several device streams and the batched
+            launches' stream, so no single stream's events cover it); max
+            over ranks
   e2e       ms per DFA by wall clock around the public call (host automaton in,
             bounds + word out)
   roofline  the kernel class with the most device time in one profiled step:
@@ -228,6 +231,36 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def learned_vs_plain(ctx, count: int) -> dict:
+    """The learned-bound comparison on the first `count` n = 384 bench automata,
+    one at a time, wall seconds per automaton: the plain GPU bidirectional
+    search (the configs/exact.json Exact entry, no beam) at the reference's
+    12 GB budget and at a budget sized to the GPU (200 GB), and
+    LearnedBeam(4096)+Exact at 12 GB.  Every run must reach the exact length."""
+    import synchrowords_gb300 as sw
+    from synchrowords_gb300.generate import random_dfa
+    big = PLAN_PLAIN_EXACT.replace('"12 * 1024"', '"200 * 1024"')
+    out = {"n": 384, "automata": [], "plans": {"plain_12gb": "Exact (configs/exact.json entry, 12 GB)",
+                                               "plain_gpu_budget": "Exact, max_memory_mb 200 GB",
+                                               "learned": "LearnedBeam(4096)+Exact (12 GB)"}}
+    for seed in range(1, count + 1):
+        d = random_dfa(384, 2, seed)
+        rec = {"seed": seed}
+        for name, plan in (("plain_12gb", PLAN_PLAIN_EXACT), ("plain_gpu_budget", big), ("learned", PLAN_LEARNED_EXACT)):
+            t0 = time.perf_counter()
+            r = ctx.solve(d, 384, 2, plan)
+            dt = time.perf_counter() - t0
+            if r.lower != r.upper or r.word is None:
+                raise RuntimeError(f"{name}: bounds [{r.lower}, {r.upper}] are not an exact length")
+            rec[name] = {"s": round(dt, 3), "length": r.upper}
+        if len({rec[k]["length"] for k in out["plans"]}) != 1:
+            raise RuntimeError(f"lengths differ between plans: {rec}")
+        rec["speedup_vs_plain_12gb"] = round(rec["plain_12gb"]["s"] / rec["learned"]["s"], 2)
+        rec["speedup_vs_plain_gpu_budget"] = round(rec["plain_gpu_budget"]["s"] / rec["learned"]["s"], 2)
+        out["automata"].append(rec)
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
     import synchrowords_gb300 as sw
@@ -243,9 +276,10 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
-    tuned = None
+    tuned = tuned_c = None
     if args.autotune:
         tuned = ctx.autotune_batch(dfas, plan)  # untimed; keeps the fastest tuning on ctx
+        tuned_c = ctx.autotune_cluster(dfas, plan)
     step_workers = 0 if args.autotune else args.streams
 
     def one_step():
@@ -266,23 +300,21 @@ def run_ours(args, world, rank, local):
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
-    dev_ms, wall_ms, launches = [], [], 0
+    dev_ms, wall_ms, launches, batched_ms = [], [], 0, 0.0
     lengths = None
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             flush.zero_()
             torch.cuda.synchronize()
             barrier(world)
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
             t0 = time.perf_counter()
             l, lengths = one_step()
             t1 = time.perf_counter()
-            e1.record(stream)
             torch.cuda.synchronize()
+            t2 = time.perf_counter()
             launches += l
-            dev_ms.append(e0.elapsed_time(e1))
+            batched_ms += ctx.last_batch_profile()["device_ms"]
+            dev_ms.append((t2 - t0) * 1000.0)
             wall_ms.append((t1 - t0) * 1000.0)
     barrier(world)
     dev_total = barrier_max(sum(dev_ms), world)
@@ -335,7 +367,12 @@ def run_ours(args, world, rank, local):
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
         "config": {"workload": desc, "n": n, "k": k, "dfas_per_step_per_gpu": count, "plan": plan_name(plan),
                    "streams": args.streams if not args.autotune else ctx.get_batch_tuning()["workers"],
-                   "batch_tuning": dict(ctx.get_batch_tuning(), autotune_ms=tuned["ms"] if tuned else None),
+                   "batch_tuning": dict(ctx.get_batch_tuning(), autotune_ms=tuned["ms"] if tuned else None,
+                                        cluster_autotune_ms=tuned_c["ms"] if tuned_c else None),
+                   "routes": {k: v for k, v in ctx.last_batch_profile().items()
+                              if k in ("small_solved", "cluster_solved", "streamed")},
+                   "batched_launch_ms_per_step": round(batched_ms / args.steps, 3),
+                   "value_timing": "wall clock between device-wide synchronisations around each step",
                    "l2": "flushed (256 MB write) before every timed step", "per_gpu_ms_per_dfa": round(value, 4)},
         "e2e": {"value": round(e2e, 4), "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": roofline,
@@ -348,6 +385,8 @@ def run_ours(args, world, rank, local):
     }
     if cpu is not None:
         line["cpu_baseline"] = cpu
+    if args.learned_vs_plain:
+        line["learned_vs_plain"] = learned_vs_plain(ctx, args.learned_vs_plain)
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -365,6 +404,9 @@ def main():
     ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
     ap.add_argument("--autotune", action="store_true",
                     help="before the warm-up, tune the batch's worker count and batched-launch limit on the workload")
+    ap.add_argument("--learned-vs-plain", type=int, default=0, metavar="N",
+                    help="also solve the first N n=384 automata plainly (12 GB and GPU-sized budgets) and with the "
+                         "learned bound, and report their wall times (minutes per automaton; off by default)")
     ap.add_argument("--instances", type=int, default=0,
                     help="solve only the first N DFAs of the workload (profiling runs; 0 = all)")
     args = ap.parse_args()

@@ -261,6 +261,20 @@ int sw_autotune_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, c
                       uint32_t n_workers, const double* limit_candidates, uint32_t n_limits, uint32_t reps,
                       double* ms, sw_batch_tuning* best);
 
+/* Cluster-launch autotuner: times the batch (wall clock, best of `reps`)
+ * first at each candidate cluster_size (CTAs per automaton, 1..16) with the
+ * current cluster_limit, then at each candidate cluster_limit (n * log2(k)
+ * bound of the automata the cluster launch takes; -1 = none) with the best
+ * size, and keeps the fastest pair in the context's tuning (workers and
+ * batched_limit unchanged).  NULL candidate lists use the defaults (sizes
+ * 2, 4, 8, 16; limits -1, 128, 160, 200).  ms (if not NULL) receives
+ * n_sizes + n_limits times; *best the chosen tuning.  No counterpart in the
+ * reference. */
+int sw_autotune_cluster(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                        const char* plan_json, sw_result* results, const int32_t* size_candidates, uint32_t n_sizes,
+                        const double* limit_candidates, uint32_t n_limits, uint32_t reps, double* ms,
+                        sw_batch_tuning* best);
+
 /* ---- measurement --------------------------------------------------------
  * No counterpart in the reference (its timers are host RAII timers,
  * synchrolib/utils/timer.hpp:9-41).  Between sw_profile_begin and

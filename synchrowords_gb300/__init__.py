@@ -161,6 +161,10 @@ def load_library():
     lib.sw_get_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
     lib.sw_set_batch_tuning.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchTuning)]
     lib.sw_batch_last_profile.argtypes = [ctypes.c_void_p, ctypes.POINTER(_BatchProfile)]
+    lib.sw_autotune_cluster.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
+                                        ctypes.POINTER(_Result), ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_BatchTuning)]
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                                      ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_void_p]
@@ -440,6 +444,33 @@ class Context:
                 "cluster_size": int(best.cluster_size), "cluster_limit": float(best.cluster_limit),
                 "ms": {"workers": {int(w): float(t) for w, t in zip(wc, ms[:len(wc)])},
                        "batched_limit": {float(x): float(t) for x, t in zip(lc, ms[len(wc):])}}}
+
+    def autotune_cluster(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: str,
+                         sizes: Optional[Sequence[int]] = None, limits: Optional[Sequence[float]] = None,
+                         reps: int = 1) -> dict:
+        """Time the batch at each candidate cluster size (CTAs per automaton of
+        the cluster launch), then at each candidate cluster limit (n * log2 k
+        of the automata it takes), and keep the fastest as this context's
+        tuning.  Returns the tuning plus {"ms": {"cluster_size": {s: ms},
+        "cluster_limit": {limit: ms}}}."""
+        if len(automata) == 0:
+            raise ValueError("empty batch")
+        ns, ks, deltas, res, words, offs = self._batch_buffers(automata)
+        sc = np.ascontiguousarray(np.asarray(sizes if sizes is not None else (2, 4, 8, 16), dtype=np.int32))
+        lc = np.ascontiguousarray(np.asarray(limits if limits is not None else (-1.0, 128.0, 160.0, 200.0),
+                                             dtype=np.float64))
+        ms = np.zeros(len(sc) + len(lc), dtype=np.float64)
+        best = _BatchTuning()
+        f64 = ctypes.POINTER(ctypes.c_double)
+        _check(self._lib.sw_autotune_cluster(self._h, len(automata), deltas.ctypes.data_as(_U32P),
+                                             ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P), plan_json.encode(),
+                                             res, sc.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(sc),
+                                             lc.ctypes.data_as(f64), len(lc), reps, ms.ctypes.data_as(f64),
+                                             ctypes.byref(best)))
+        return {"workers": int(best.workers), "batched_limit": float(best.batched_limit),
+                "cluster_size": int(best.cluster_size), "cluster_limit": float(best.cluster_limit),
+                "ms": {"cluster_size": {int(s): float(t) for s, t in zip(sc, ms[:len(sc)])},
+                       "cluster_limit": {float(x): float(t) for x, t in zip(lc, ms[len(sc):])}}}
 
     def get_batch_tuning(self) -> dict:
         t = _BatchTuning()

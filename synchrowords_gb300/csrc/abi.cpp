@@ -673,6 +673,83 @@ int sw_autotune_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, c
   return SW_OK;
 }
 
+int sw_autotune_cluster(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                        const char* plan_json, sw_result* results, const int32_t* size_candidates, uint32_t n_sizes,
+                        const double* limit_candidates, uint32_t n_limits, uint32_t reps, double* ms,
+                        sw_batch_tuning* best) {
+  if (!ctx || !plan_json || (count && (!deltas || !ns || !ks || !results)))
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (count == 0) return fail(SW_ERR_INVALID_ARGUMENT, "empty batch");
+  static const int32_t kSizes[4] = {2, 4, 8, 16};
+  static const double kLimits[4] = {-1.0, 128.0, 160.0, 200.0};
+  if (!size_candidates) {
+    size_candidates = kSizes;
+    n_sizes = 4;
+  }
+  if (!limit_candidates) {
+    limit_candidates = kLimits;
+    n_limits = 4;
+  }
+  if (n_sizes == 0 || n_limits == 0) return fail(SW_ERR_INVALID_ARGUMENT, "empty candidate list");
+  for (uint32_t c = 0; c < n_sizes; ++c)
+    if (size_candidates[c] < 1 || size_candidates[c] > 16) return fail(SW_ERR_INVALID_ARGUMENT, "cluster size must be 1..16");
+  reps = std::max<uint32_t>(reps, 1);
+  const sw_batch_tuning saved = ctx->tuning;
+  auto run = [&](const sw_batch_tuning& t, double& out) -> int {
+    ctx->tuning = t;
+    for (uint32_t r = 0; r < reps; ++r) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const int rc = sw_solve_batch(ctx, count, deltas, ns, ks, plan_json, results, 0);
+      if (rc != SW_OK) return rc;
+      const double ms_run = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (r == 0 || ms_run < out) out = ms_run;
+    }
+    return SW_OK;
+  };
+  // coordinate descent: cluster size with the current limit, then the limit
+  sw_batch_tuning cur = saved, top = saved;
+  double top_ms = 0;
+  bool have = false;
+  for (uint32_t c = 0; c < n_sizes; ++c) {
+    cur.cluster_size = size_candidates[c];
+    double t = 0;
+    const int rc = run(cur, t);
+    if (rc != SW_OK) {
+      ctx->tuning = saved;
+      return rc;
+    }
+    if (ms) ms[c] = t;
+    if (!have || t < top_ms) {
+      top_ms = t;
+      top = cur;
+      have = true;
+    }
+  }
+  cur = top;
+  const double first_limit = top.cluster_limit, first_ms = top_ms;
+  for (uint32_t c = 0; c < n_limits; ++c) {
+    cur.cluster_limit = limit_candidates[c];
+    if (cur.cluster_limit == first_limit) {  // measured in the first pass
+      if (ms) ms[n_sizes + c] = first_ms;
+      continue;
+    }
+    double t = 0;
+    const int rc = run(cur, t);
+    if (rc != SW_OK) {
+      ctx->tuning = saved;
+      return rc;
+    }
+    if (ms) ms[n_sizes + c] = t;
+    if (t < top_ms) {
+      top_ms = t;
+      top = cur;
+    }
+  }
+  ctx->tuning = top;
+  if (best) *best = top;
+  return SW_OK;
+}
+
 int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k, const char* plan_json,
                   sw_result* r) {
   sw_plan plan;

@@ -66,4 +66,10 @@ def test_autotune_batch_picks_candidates_and_keeps_results(native_lib):
         prof = ctx.last_batch_profile()
         if cs >= 0:
             assert prof["cluster_solved"] > 0 and prof["small_solved"] == 0, prof
+    # the cluster autotuner: candidates timed, the choice kept, answers unchanged
+    tuned = ctx.autotune_cluster(autos, PLAN, sizes=(4, 8), limits=(-1.0, 160.0), reps=1)
+    assert tuned["cluster_size"] in (4, 8) and tuned["cluster_limit"] in (-1.0, 160.0)
+    assert set(tuned["ms"]["cluster_size"]) == {4, 8} and set(tuned["ms"]["cluster_limit"]) == {-1.0, 160.0}
+    assert ctx.get_batch_tuning()["cluster_size"] == tuned["cluster_size"]
+    check_against_golden(autos, ctx.solve_batch(autos, PLAN))
     ctx.close()

@@ -286,3 +286,32 @@ def test_cluster_launch_random_sizes_against_the_streamed_path(native_lib):
             assert (r.lower, r.upper) == (ref.lower, ref.upper), (n, k)
         if r.lower == r.upper:  # else both routes stopped at the plan's memory budget with the same bounds
             check_word(d, n, k, r)
+
+
+LEARNED_EXACT = json.dumps({
+    "upper_bound": "1ULL * (AUT_N - 1) * (AUT_N - 1) + 1",
+    "algorithms": [
+        {"name": "LearnedBeam", "config": {"beam_size": "4096", "order": "model"}},
+        {"name": "Exact", "config": {"dfs_min_list_size": "8192", "bfs_small_list_size": "AUT_N * AUT_K",
+                                     "dfs": True, "dfs_shortcut": True, "max_memory_mb": "12 * 1024"}}]})
+
+
+@pytest.mark.parametrize("n", [320, 384])
+def test_c5_learned_plan_matches_reference(ctx, n):
+    """The sixteen n = 320 / 384 bench automata with the learned bound:
+    LearnedBeam(4096, the packaged distance model) then the configs/exact.json
+    Exact entry, as the bench's n384_learned workload runs them.  The bound only
+    changes how the exact search proceeds: every length equals the compiled
+    reference's (tests/golden/random_n{320,384}.json, Beam(dynamic)+Exact) and
+    every word is verified."""
+    import synchrowords_gb300 as sw
+    if not sw.DEFAULT_MODEL.exists():
+        pytest.skip("no packaged model")
+    g = _fixture(f"random_n{n}.json")
+    ref = g["reference"]["beam_exact"]
+    autos = [(n, 2, random_dfa(n, 2, s)) for s in g["seeds"]]
+    res = ctx.solve_batch(autos, LEARNED_EXACT, workers=8)
+    for (nn, k, d), r, want in zip(autos, res, ref["results"]):
+        assert (r.lower, r.upper) == (want["lower"], want["upper"])
+        assert r.runs[0][0] == "LearnedBeam"
+        check_word(d, nn, k, r)

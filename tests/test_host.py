@@ -55,6 +55,7 @@ def test_batch_entry_points_reject_null_arguments(native_lib):
     assert b"NULL" in lib.sw_last_error()
     assert lib.sw_solve_batch(None, 1, None, None, None, b"{}", None, 0) == -1
     assert lib.sw_autotune_batch(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
+    assert lib.sw_autotune_cluster(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
     assert b"NULL" in lib.sw_last_error()
 
 
