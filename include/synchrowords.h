@@ -62,7 +62,18 @@ typedef struct {
   uint64_t max_memory_mb;       /* "max_memory_mb" (default 2048): device budget of the lists */
   uint64_t dfs_min_list_size;   /* "dfs_min_list_size" (default 10000) */
   uint64_t bfs_small_list_size; /* "bfs_small_list_size" (default AUT_N * 16) */
+  /* "reductions" (no reference key; the reference always reduces): when the
+   * device search drops sets dominated by a visited set or by a proper subset
+   * in their layer (meet_in_the_middle.cpp:195-237, 264-337).  Lengths never
+   * depend on it.  SW_REDUCE_AUTO ("auto", default): when the upper bound is
+   * backed by a word or the lists pass a quarter of max_memory_mb;
+   * SW_REDUCE_ALWAYS ("always"); SW_REDUCE_MEMORY ("memory"): only past a
+   * quarter of max_memory_mb. */
+  int32_t reductions;
 } sw_exact_config;
+#define SW_REDUCE_AUTO 0
+#define SW_REDUCE_ALWAYS 1
+#define SW_REDUCE_MEMORY 2
 
 /* Evaluated Beam defines (synchrolib/algorithm/beam/config.hpp:23-44). */
 typedef struct {

@@ -43,7 +43,7 @@ class SynchroError(RuntimeError):
 class _ExactCfg(ctypes.Structure):
     _fields_ = [("dfs", ctypes.c_int32), ("dfs_shortcut", ctypes.c_int32), ("strict_memory_limit", ctypes.c_int32),
                 ("max_memory_mb", ctypes.c_uint64), ("dfs_min_list_size", ctypes.c_uint64),
-                ("bfs_small_list_size", ctypes.c_uint64)]
+                ("bfs_small_list_size", ctypes.c_uint64), ("reductions", ctypes.c_int32)]
 
 
 class _BeamCfg(ctypes.Structure):

@@ -759,7 +759,9 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     // self reduction only where it pays: a word-backed bound (the bounded
     // phase expands B from its size at the switch) or lists past a quarter
     // of the memory budget
-    E.self_check = E.visited_subsets = b.has_word || 4 * (live + next) > budget;
+    const bool pressure = 4 * (live + next) > budget;
+    E.self_check = E.visited_subsets = cfg.reductions == SW_REDUCE_ALWAYS ||
+                                       (cfg.reductions == SW_REDUCE_AUTO && b.has_word) || pressure;
     E.step(X, fwd, W, n, k, /*dominance=*/!bounded);
     // projected branching of the bounded levels: distinct children per parent
     // before pruning, never below 1.5, plus 10% margin

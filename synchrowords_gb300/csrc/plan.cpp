@@ -771,6 +771,20 @@ void plan_from_json(const std::string& text, uint32_t n, uint32_t k, sw_plan* ou
       alg.exact.max_memory_mb = value_of(cfg, "max_memory_mb", "2048", n, k).as_u64();
       alg.exact.dfs_min_list_size = value_of(cfg, "dfs_min_list_size", "10000", n, k).as_u64();
       alg.exact.bfs_small_list_size = value_of(cfg, "bfs_small_list_size", "AUT_N * 16", n, k).as_u64();
+      std::string red = "auto";
+      if (cfg && cfg->get("reductions")) {
+        const Json* r = cfg->get("reductions");
+        if (r->type != Json::String) throw std::runtime_error("reductions value not in [auto, always, memory]");
+        red = r->str;
+      }
+      if (red == "auto")
+        alg.exact.reductions = SW_REDUCE_AUTO;
+      else if (red == "always")
+        alg.exact.reductions = SW_REDUCE_ALWAYS;
+      else if (red == "memory")
+        alg.exact.reductions = SW_REDUCE_MEMORY;
+      else
+        throw std::runtime_error("reductions value not in [auto, always, memory]");
     } else if (name == "Beam") {  // synchrolib/algorithm/beam/config.hpp:23-44
       alg.kind = SW_ALGO_BEAM;
       alg.beam.beam_size = (uint32_t)value_of(cfg, "beam_size", "std::log2(AUT_N)", n, k).as_u64();
