@@ -440,15 +440,19 @@ __global__ void __launch_bounds__(kCtThreads, 1)
       const u32 units = chunks * fslices;
       my_pairs += (u64)nF * nB;
       u32 staged = 0xffffffffu;
+      // Block barriers only around restaging a chunk (every warp of the CTA
+      // walks the same unit sequence); a warp that sees the meet flag set
+      // skips its remaining work but still takes part in those barriers.
+      bool met = false;
       for (u32 u = rank; u < units; u += CS) {
-        if (tid == 0) s_flag = ld_volatile(&ctl->found);
-        __syncthreads();
-        if (s_flag != 0) break;  // block-uniform
         const u32 chunk = u / fslices, fs = u - chunk * fslices;
         const u32 r0 = chunk * kCtChunkRows;
         const u32 rows = min(kCtChunkRows, nB - r0);
         const u32 groups = (rows + 31) / 32;
         if (chunk != staged) {
+          if (tid == 0) s_flag = ld_volatile(&ctl->found);
+          __syncthreads();  // every warp is done with the previous chunk
+          if (s_flag != 0) break;  // block-uniform: the meet was found
           // transpose: bit j of s_col[q * kCtGroups + g] says state q lies in
           // B_{r0 + 32 g + j}; warp per 32-row group, one ballot per state
           for (u32 g = warp; g < groups; g += kCtWarps) {
@@ -480,6 +484,11 @@ __global__ void __launch_bounds__(kCtThreads, 1)
         // the warp takes them one by one (broadcast by shuffle) and ANDs the
         // bitmaps of each set's states; lane l owns the chunk's 32-row words
         // 4l .. 4l + 3 (one 16-byte shared load per state)
+        if (!met) {
+          u32 fl = lane == 0 ? ld_volatile(&ctl->found) : 0u;
+          met = __shfl_sync(0xffffffffu, fl, 0) != 0;
+        }
+        if (met) continue;
         const u32 fw0 = fs * kCtFSlice + warp * 32;
         const u32 fw1 = min(nF, fw0 + 32);
         u64 myf[W];
@@ -525,7 +534,6 @@ __global__ void __launch_bounds__(kCtThreads, 1)
             break;
           }
         }
-        __syncthreads();  // the staged chunk stays until every warp is done with it
       }
       cluster_barrier();
       lap(3);
