@@ -1,101 +1,197 @@
 // Kernels of the learned distance model (mlp.cuh).
 //
-// The generic product C = A · B is tiled 64 x 64 x 32 per block of four warps;
-// each warp owns 16 rows of the tile and issues mma.sync m16n8k16 (bf16 in,
-// fp32 accumulate) over the tile's eight 8-column slices.  Operands are
-// staged in shared memory through strided loads so that the same kernel
-// serves the forward products and the transposed products of the backward
-// pass.  Fragment layouts are the ones PTX defines for m16n8k16 with
-// .row.col: with g = lane / 4 and t = lane % 4, A registers hold (g, 2t..2t+1),
-// (g+8, 2t..), (g, 2t+8..), (g+8, 2t+8..); B registers hold (k = 2t..2t+1,
-// n = g) and (k = 2t+8.., n = g); C holds (g, 2t..2t+1) and (g+8, 2t..2t+1).
+// The generic product C = A · B runs on the fifth-generation tensor cores:
+// one CTA of four warps owns a 128-row tile of C with all of its N (64 or 128)
+// columns.  Per 64-deep slice of K the warps stage A (128 x 64) and B
+// (N x 64) in shared memory as bf16 in the canonical K-major layout without
+// swizzle (8 x 8 "core matrices" of 128 contiguous bytes, K-adjacent cores
+// 128 bytes apart, 8-row groups 1024 bytes apart); one thread then issues four
+// tcgen05.mma (kind::f16: bf16 x bf16 -> fp32, M = 128, K = 16 each) into a
+// TMEM accumulator of N columns and commits them to an mbarrier.  At the end
+// the warps read their 32 accumulator rows back with tcgen05.ld.  Operands are
+// read through strided views, so the same kernel serves the forward products
+// and the transposed products of the backward pass.  Every wait is bounded: a
+// wait that runs out sets an error word (tc_error()), the CTA frees its TMEM
+// and stops.
 #include "mlp.cuh"
 
 namespace sw {
 namespace mlp {
 
 namespace {
-constexpr int kBM = 64, kBN = 64, kBK = 32, kPad = 8;
+constexpr int kTM = 128;     // rows of C per CTA (the MMA's M)
+constexpr int kTK = 64;      // K per staged slice (four MMAs of K = 16)
+constexpr int kMaxN = 128;   // columns of C per CTA (the MMA's N; the TMEM columns)
+constexpr int kTcThreads = 128;
+constexpr u32 kTcWaitLimit = 1u << 24;
+// shared memory: A slice, B slice (bf16, core-matrix layout), then the mbarrier and the TMEM address.
+// A CTA asks for 60 KB so that at most three share an SM: three accumulators
+// of 128 columns fit the SM's 512 TMEM columns, so an allocation never waits.
+constexpr int kSmemA = kTM * kTK * 2;
+constexpr int kSmemB = kMaxN * kTK * 2;
+constexpr int kTcSmem = 60 * 1024;
+static_assert(kSmemA + kSmemB + 64 <= kTcSmem, "slices and barrier fit the CTA's shared memory");
 
-__device__ inline uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+__device__ u32 g_tc_error = 0;
+
+__device__ __forceinline__ u32 sm_addr(const void* p) { return (u32)__cvta_generic_to_shared(p); }
+
+// byte offset of element (row r, k) of a slice in the canonical no-swizzle
+// K-major layout: core matrix (r / 8, k / 8), 16-byte rows inside it
+__device__ __forceinline__ u32 core_offset(int r, int k) {
+  return (u32)((r >> 3) * 1024 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// tcgen05 shared-memory descriptor: start address, leading-dimension byte
+// offset (K-adjacent core matrices), stride byte offset (8-row groups),
+// descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(u32 addr) {
+  const uint64_t start = (addr & 0x3FFFFu) >> 4;
+  const uint64_t lbo = 128u >> 4, sbo = 1024u >> 4;
+  return start | (lbo << 16) | (sbo << 32) | (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: fp32 accumulator, bf16 A and B, both
+// K-major, N >> 3 and M >> 4
+__device__ __forceinline__ u32 instr_desc(int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((u32)(n >> 3) << 17) | ((u32)(kTM >> 4) << 24);
+}
+
+__device__ __forceinline__ bool bar_wait(u32 bar, u32 parity) {
+  for (u32 it = 0; it < kTcWaitLimit; ++it) {
+    u32 ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 }  // namespace
 
-__global__ void __launch_bounds__(128) k_gemm(View A, View B, float* __restrict__ C, int ldc, int M, int N, int K,
-                                              int k_slice, int atomic) {
-  __shared__ __nv_bfloat16 sA[kBM][kBK + kPad];  // [row][k]
-  __shared__ __nv_bfloat16 sB[kBN][kBK + kPad];  // [col][k]
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int g = lane >> 2, t = lane & 3;
-  const int i0 = blockIdx.y * kBM, j0 = blockIdx.x * kBN;
+__global__ void __launch_bounds__(kTcThreads) k_gemm_tc(View A, View B, float* __restrict__ C, int ldc, int M, int N,
+                                                        int K, int k_slice, int atomic) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + kSmemA;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + kSmemA + kSmemB);
+  u32* tmem_slot = reinterpret_cast<u32*>(smem + kSmemA + kSmemB + 16);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int i0 = blockIdx.x * kTM;
   const int kb = blockIdx.z * k_slice, ke = min(K, kb + k_slice);
-  const __nv_bfloat16 zero = __float2bfloat16(0.0f);
-  float acc[8][4];
-#pragma unroll
-  for (int s = 0; s < 8; ++s)
-#pragma unroll
-    for (int r = 0; r < 4; ++r) acc[s][r] = 0.0f;
-  for (int k0 = kb; k0 < ke; k0 += kBK) {
-    for (int e = tid; e < kBM * kBK; e += 128) {
-      const int r = e / kBK, kk = e % kBK;
-      const int i = i0 + r, k = k0 + kk;
-      sA[r][kk] = (i < M && k < ke) ? A.p[(long long)i * A.si + (long long)k * A.sk] : zero;
-    }
-    for (int e = tid; e < kBN * kBK; e += 128) {
-      const int c = e / kBK, kk = e % kBK;
-      const int j = j0 + c, k = k0 + kk;
-      sB[c][kk] = (j < N && k < ke) ? B.p[(long long)k * B.si + (long long)j * B.sk] : zero;
-    }
-    __syncthreads();
-#pragma unroll
-    for (int ks = 0; ks < kBK; ks += 16) {
-      const int r = warp * 16 + g;
-      uint32_t a[4];
-      a[0] = pack2(sA[r][ks + 2 * t], sA[r][ks + 2 * t + 1]);
-      a[1] = pack2(sA[r + 8][ks + 2 * t], sA[r + 8][ks + 2 * t + 1]);
-      a[2] = pack2(sA[r][ks + 2 * t + 8], sA[r][ks + 2 * t + 9]);
-      a[3] = pack2(sA[r + 8][ks + 2 * t + 8], sA[r + 8][ks + 2 * t + 9]);
-#pragma unroll
-      for (int s = 0; s < 8; ++s) {
-        const int c = s * 8 + g;
-        uint32_t b0 = pack2(sB[c][ks + 2 * t], sB[c][ks + 2 * t + 1]);
-        uint32_t b1 = pack2(sB[c][ks + 2 * t + 8], sB[c][ks + 2 * t + 9]);
-        asm volatile(
-            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-            "{%0,%1,%2,%3};\n"
-            : "+f"(acc[s][0]), "+f"(acc[s][1]), "+f"(acc[s][2]), "+f"(acc[s][3])
-            : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-      }
-    }
-    __syncthreads();
+  const u32 ncols = N <= 64 ? 64u : 128u;  // TMEM columns: a power of two >= 32
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sm_addr(bar)) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sm_addr(tmem_slot)),
+                 "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const u32 tmem = *tmem_slot;
+  const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+  u32 parity = 0;
+  bool ok = true, first = true;
+  for (int k0 = kb; k0 < ke && ok; k0 += kTK) {
+    // stage the slices (rows / columns past M, N and k past the slice are zero)
+    for (int e = tid; e < kTM * kTK; e += kTcThreads) {
+      const int r = e / kTK, kk = e % kTK, i = i0 + r, k = k0 + kk;
+      const __nv_bfloat16 v = (i < M && k < ke) ? A.p[(long long)i * A.si + (long long)k * A.sk] : zero;
+      *reinterpret_cast<__nv_bfloat16*>(sA + core_offset(r, kk)) = v;
+    }
+    for (int e = tid; e < (int)ncols * kTK; e += kTcThreads) {
+      const int c = e / kTK, kk = e % kTK, k = k0 + kk;
+      const __nv_bfloat16 v = (c < N && k < ke) ? B.p[(long long)k * B.si + (long long)c * B.sk] : zero;
+      *reinterpret_cast<__nv_bfloat16*>(sB + core_offset(c, kk)) = v;
+    }
+    // the tensor cores read shared memory through the async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const u32 idesc = instr_desc((int)ncols);
 #pragma unroll
-  for (int s = 0; s < 8; ++s)
+      for (int s = 0; s < kTK / 16; ++s) {
+        const uint64_t da = smem_desc(sm_addr(sA) + s * 256);  // K = 16 s: two cores of 128 bytes further
+        const uint64_t db = smem_desc(sm_addr(sB) + s * 256);
+        const u32 acc = (first && s == 0) ? 0u : 1u;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+            "l"(da), "l"(db), "r"(idesc), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(sm_addr(bar))
+                   : "memory");
+    }
+    first = false;
+    // the MMAs must have read the slices before they are overwritten
+    ok = bar_wait(sm_addr(bar), parity);
+    parity ^= 1u;
+    ok = __syncthreads_and(ok);
+  }
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (!ok) {
+    if (tid == 0) atomicExch(&g_tc_error, 1u);
+  } else if (!first) {
+    // warp w reads accumulator rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns at a time
+    const int i = i0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < (int)ncols; c0 += 16) {
+      u32 v[16];
+      const u32 taddr = tmem + ((u32)(warp * 32) << 16) + (u32)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+            "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (i < M) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int i = i0 + warp * 16 + g + (r >= 2 ? 8 : 0);
-      const int j = j0 + s * 8 + 2 * t + (r & 1);
-      if (i < M && j < N) {
-        float* dst = C + (long long)i * ldc + j;
-        if (atomic)
-          atomicAdd(dst, acc[s][r]);
-        else
-          *dst = acc[s][r];
+        for (int j = 0; j < 16; ++j) {
+          const int col = c0 + j;
+          if (col < N) {
+            float* dst = C + (long long)i * ldc + col;
+            if (atomic)
+              atomicAdd(dst, __uint_as_float(v[j]));
+            else
+              *dst = __uint_as_float(v[j]);
+          }
+        }
       }
     }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols) : "memory");
 }
 
 void gemm(View A, View B, float* C, int ldc, int M, int N, int K, bool atomic, int split, cudaStream_t s) {
   if (M <= 0 || N <= 0 || K <= 0) return;
+  if (N > kMaxN) throw std::invalid_argument("mlp gemm: N above 128");
   split = std::max(1, split);
   int slice = (K + split - 1) / split;
-  slice = (slice + kBK - 1) / kBK * kBK;
+  slice = (slice + kTK - 1) / kTK * kTK;
   split = (K + slice - 1) / slice;
   if (split > 1) atomic = true;
-  dim3 grid((N + kBN - 1) / kBN, (M + kBM - 1) / kBM, split);
-  k_gemm<<<grid, 128, 0, s>>>(A, B, C, ldc, M, N, K, slice, atomic ? 1 : 0);
+  ensure_smem_limit((const void*)k_gemm_tc, kTcSmem);
+  dim3 grid((M + kTM - 1) / kTM, 1, split);
+  k_gemm_tc<<<grid, kTcThreads, kTcSmem, s>>>(A, B, C, ldc, M, N, K, slice, atomic ? 1 : 0);
   SW_LAUNCH_CHECK();
+}
+
+bool tc_error() {
+  u32 v = 0;
+  SW_CUDA(cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(u32)));
+  return v != 0;
 }
 
 __global__ void k_bits_to_dense(const u64* __restrict__ rows, int W, int n, u32 count, __nv_bfloat16* out, int ld) {

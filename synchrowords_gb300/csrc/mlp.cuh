@@ -5,7 +5,7 @@
 //   y   = h2 · w3 + b3                            predicted shortest merge length
 // feat is a fixed per-state feature vector of the automaton (automaton.cpp),
 // so one trained model applies to automata of any size.  Dense products run
-// on the tensor cores (mma.sync m16n8k16, bf16 inputs, fp32 accumulation);
+// on the tensor cores (tcgen05.mma, bf16 inputs, fp32 accumulation in TMEM);
 // master weights, gradients and Adam moments are fp32.
 #pragma once
 #include <cuda_bf16.h>
@@ -36,10 +36,13 @@ struct View {
   long long si, sk;
 };
 
-// C[i*ldc + j] (= or +=) sum_k A(i,k) B(k,j) for i < M, j < N; `atomic`
+// C[i*ldc + j] (= or +=) sum_k A(i,k) B(k,j) for i < M, j < N <= 128; `atomic`
 // accumulates with atomicAdd (required when split > 1: K is cut in `split`
 // slices, one per grid z).
 void gemm(View A, View B, float* C, int ldc, int M, int N, int K, bool atomic, int split, cudaStream_t s);
+// True once a product's bounded wait for its tensor-core work ran out (its
+// results are then incomplete); synchronises with the device.
+bool tc_error();
 
 // Set rows (device layout, W words) -> dense 0/1 bf16 rows of width ld (>= n).
 void bits_to_dense(const u64* rows, int W, int n, u32 count, __nv_bfloat16* out, int ld, cudaStream_t s);
