@@ -1,14 +1,15 @@
 // Kernels of the learned distance model (mlp.cuh).
 //
 // The generic product C = A · B runs on the fifth-generation tensor cores:
-// one CTA of four warps owns a 128-row tile of C with all of its N (64 or 128)
-// columns.  Per 64-deep slice of K the warps stage A (128 x 64) and B
+// one CTA of eight warps owns a 128-row tile of C with all of its N (64 or
+// 128) columns.  Per 64-deep slice of K the warps stage A (128 x 64) and B
 // (N x 64) in shared memory as bf16 in the canonical K-major layout without
 // swizzle (8 x 8 "core matrices" of 128 contiguous bytes, K-adjacent cores
 // 128 bytes apart, 8-row groups 1024 bytes apart); one thread then issues four
 // tcgen05.mma (kind::f16: bf16 x bf16 -> fp32, M = 128, K = 16 each) into a
 // TMEM accumulator of N columns and commits them to an mbarrier.  At the end
-// the warps read their 32 accumulator rows back with tcgen05.ld.  Operands are
+// each warp reads 32 accumulator rows (its TMEM lanes) and half of the
+// columns back with tcgen05.ld.  Contiguous operands move as 16-byte loads.  Operands are
 // read through strided views, so the same kernel serves the forward products
 // and the transposed products of the backward pass.  Every wait is bounded: a
 // wait that runs out sets an error word (tc_error()), the CTA frees its TMEM
@@ -22,7 +23,7 @@ namespace {
 constexpr int kTM = 128;     // rows of C per CTA (the MMA's M)
 constexpr int kTK = 64;      // K per staged slice (four MMAs of K = 16)
 constexpr int kMaxN = 128;   // columns of C per CTA (the MMA's N; the TMEM columns)
-constexpr int kTcThreads = 128;
+constexpr int kTcThreads = 256;  // eight warps stage; warps w and w + 4 share TMEM lanes 32 (w % 4) ..
 constexpr u32 kTcWaitLimit = 1u << 24;
 // shared memory: A slice, B slice (bf16, core-matrix layout), then the mbarrier and the TMEM address.
 // A CTA asks for 60 KB so that at most three share an SM: three accumulators
@@ -97,19 +98,55 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(View A, View B, float* _
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const u32 tmem = *tmem_slot;
   const __nv_bfloat16 zero = __float2bfloat16(0.0f);
+  // rows of A (columns of B) contiguous along the staged dimension and 16-byte aligned: vector loads
+  const bool vecA = A.sk == 1 && A.si % 8 == 0 && ((uintptr_t)A.p & 15) == 0;
+  const bool vecB = B.sk == 1 && B.si % 8 == 0 && ((uintptr_t)B.p & 15) == 0;
   u32 parity = 0;
   bool ok = true, first = true;
   for (int k0 = kb; k0 < ke && ok; k0 += kTK) {
     // stage the slices (rows / columns past M, N and k past the slice are zero)
-    for (int e = tid; e < kTM * kTK; e += kTcThreads) {
-      const int r = e / kTK, kk = e % kTK, i = i0 + r, k = k0 + kk;
-      const __nv_bfloat16 v = (i < M && k < ke) ? A.p[(long long)i * A.si + (long long)k * A.sk] : zero;
-      *reinterpret_cast<__nv_bfloat16*>(sA + core_offset(r, kk)) = v;
+    if (vecA) {
+      // eight consecutive k of a row: one 16-byte load, one 16-byte core-matrix row
+      for (int e = tid; e < kTM * (kTK / 8); e += kTcThreads) {
+        const int r = e / (kTK / 8), kk = (e % (kTK / 8)) * 8, i = i0 + r, k = k0 + kk;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (i < M && k + 8 <= ke) {
+          v = *reinterpret_cast<const uint4*>(A.p + (long long)i * A.si + k);
+        } else if (i < M && k < ke) {
+          __nv_bfloat16 t[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) t[j] = k + j < ke ? A.p[(long long)i * A.si + k + j] : zero;
+          v = *reinterpret_cast<const uint4*>(t);
+        }
+        *reinterpret_cast<uint4*>(sA + core_offset(r, kk)) = v;
+      }
+    } else {
+      for (int e = tid; e < kTM * kTK; e += kTcThreads) {
+        const int r = e / kTK, kk = e % kTK, i = i0 + r, k = k0 + kk;
+        const __nv_bfloat16 v = (i < M && k < ke) ? A.p[(long long)i * A.si + (long long)k * A.sk] : zero;
+        *reinterpret_cast<__nv_bfloat16*>(sA + core_offset(r, kk)) = v;
+      }
     }
-    for (int e = tid; e < (int)ncols * kTK; e += kTcThreads) {
-      const int c = e / kTK, kk = e % kTK, k = k0 + kk;
-      const __nv_bfloat16 v = (c < N && k < ke) ? B.p[(long long)k * B.si + (long long)c * B.sk] : zero;
-      *reinterpret_cast<__nv_bfloat16*>(sB + core_offset(c, kk)) = v;
+    if (vecB) {
+      // eight consecutive columns of one k: one 16-byte load, eight core-matrix rows
+      for (int e = tid; e < (int)(ncols / 8) * kTK; e += kTcThreads) {
+        const int kk = e / (int)(ncols / 8), c = (e % (int)(ncols / 8)) * 8, k = k0 + kk;
+        __nv_bfloat16 t[8];
+        if (k < ke && c + 8 <= N) {
+          *reinterpret_cast<uint4*>(t) = *reinterpret_cast<const uint4*>(B.p + (long long)k * B.si + c);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) t[j] = (k < ke && c + j < N) ? B.p[(long long)k * B.si + c + j] : zero;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) *reinterpret_cast<__nv_bfloat16*>(sB + core_offset(c + j, kk)) = t[j];
+      }
+    } else {
+      for (int e = tid; e < (int)ncols * kTK; e += kTcThreads) {
+        const int c = e / kTK, kk = e % kTK, k = k0 + kk;
+        const __nv_bfloat16 v = (c < N && k < ke) ? B.p[(long long)k * B.si + (long long)c * B.sk] : zero;
+        *reinterpret_cast<__nv_bfloat16*>(sB + core_offset(c, kk)) = v;
+      }
     }
     // the tensor cores read shared memory through the async proxy
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -141,11 +178,14 @@ __global__ void __launch_bounds__(kTcThreads) k_gemm_tc(View A, View B, float* _
   if (!ok) {
     if (tid == 0) atomicExch(&g_tc_error, 1u);
   } else if (!first) {
-    // warp w reads accumulator rows 32 w .. 32 w + 31 (TMEM lanes), 16 columns at a time
-    const int i = i0 + warp * 32 + lane;
-    for (int c0 = 0; c0 < (int)ncols; c0 += 16) {
+    // warp w reads accumulator rows 32 (w % 4) .. + 31 (its TMEM lanes), half
+    // of the columns each for w < 4 and w >= 4, 16 columns at a time
+    const int q = warp & 3, half = warp >> 2;
+    const int i = i0 + q * 32 + lane;
+    const int cbeg = half * (int)(ncols / 2), cend = cbeg + (int)(ncols / 2);
+    for (int c0 = cbeg; c0 < cend; c0 += 16) {
       u32 v[16];
-      const u32 taddr = tmem + ((u32)(warp * 32) << 16) + (u32)c0;
+      const u32 taddr = tmem + ((u32)(q * 32) << 16) + (u32)c0;
       asm volatile(
           "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
           : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
