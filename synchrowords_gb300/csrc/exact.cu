@@ -50,14 +50,33 @@ struct Side {
   double unique_growth = 0;      // distinct children per parent at the last step
   KeyMap keymap;                 // sort key of this side's layers and visited list
   bool keymap_chosen = false;
+  // Layers of earlier solves, kept with their device buffers: freeing device
+  // memory synchronises the whole device, which would stall every other
+  // solve running on the GPU at the time.
+  std::vector<std::unique_ptr<Layer>> spare;
+  std::unique_ptr<Layer> new_layer() {
+    if (spare.empty()) return std::make_unique<Layer>();
+    std::unique_ptr<Layer> L = std::move(spare.back());
+    spare.pop_back();
+    L->count = L->parent_count = 0;
+    return L;
+  }
   void reset() {
     count = vis_count = 0;
     unique_growth = 0;
     keymap = KeyMap{};
     keymap_chosen = false;
+    for (auto& L : layers) spare.push_back(std::move(L));
     layers.clear();
     seed_states.clear();
   }
+};
+
+// One level of the bounded inverse phase (a chunk of parents' children).
+struct DLevel {
+  DevBuf rows, origin;
+  u32 count = 0;
+  u32 chunk_off = 0, chunk_cnt = 0;  // parent slice this level was expanded from
 };
 
 }  // namespace
@@ -173,6 +192,9 @@ class Engine {
   }
   Side F, B;
   sw_stats* st = nullptr;
+  std::vector<std::unique_ptr<DLevel>> dlevel_pool;  // the bounded phase's per-depth levels
+  // scratch of the learned beam and of Reduce, kept across calls
+  DevBuf lb_counts, lb_scores, lb_keys, lb_vals, lb_alt_k, lb_alt_v, lb_sel_rows, lb_sel_origin, red_counts;
 
   void upload_tables(const Automaton& A) {
     HostTables h = build_tables(A);
@@ -332,7 +354,7 @@ class Engine {
         st->subsets_kept += u;
         st->dfs_sets += u;
       }
-      auto L = std::make_unique<Layer>();
+      auto L = X.new_layer();
       L->origin.reserve(sizeof(u32) * std::max<u32>(u, 1));
       if (u) SW_CUDA(cudaMemcpyAsync(L->origin.p, uq_vals.p, sizeof(u32) * u, cudaMemcpyDeviceToDevice, stream));
       L->count = u;
@@ -395,7 +417,7 @@ class Engine {
     std::swap(X.rows.cap, X.rows_alt.cap);
     X.count = f;
     if (st) st->subsets_kept += f;
-    auto L = std::make_unique<Layer>();
+    auto L = X.new_layer();
     L->origin.reserve(sizeof(u32) * std::max<u32>(f, 1));
     if (f)
       SW_CUDA(cudaMemcpyAsync(L->origin.p, new_vals.p, sizeof(u32) * f, cudaMemcpyDeviceToDevice, stream));
@@ -524,11 +546,6 @@ class Engine {
 // below L (dfs.cpp:179-189), so the smallest length found is the answer.
 // ---------------------------------------------------------------------------
 namespace {
-struct DLevel {
-  DevBuf rows, origin;
-  u32 count = 0;
-  u32 chunk_off = 0, chunk_cnt = 0;  // parent slice this level was expanded from
-};
 
 struct BoundedSearch {
   Engine& E;
@@ -834,8 +851,10 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
   if (bounded && !found) {
     BoundedSearch S{E, A, W, n, k, budget, row_bytes, std::max<u64>(cfg.dfs_min_list_size, 1), max_rt, 0, {}, 0,
                     {}, {}, st};
+    S.pool.swap(E.dlevel_pool);  // levels (and their device buffers) kept across solves
     S.levels.push_back(nullptr);
     S.explore(0, 0, E.B.count, rt);
+    E.dlevel_pool.swap(S.pool);
     if (S.best) {
       found = true;
       rt = S.best;
@@ -965,7 +984,7 @@ static BeamRun beam_cutoff(Engine& E, const Automaton& A, u32 beam_size, u64 max
     E.count_launch();
     std::swap(X.rows.p, X.rows_alt.p);
     std::swap(X.rows.cap, X.rows_alt.cap);
-    auto L = std::make_unique<Layer>();
+    auto L = X.new_layer();
     L->origin.reserve(sizeof(u32) * std::max<u32>(keep, 1));
     SW_CUDA(cudaMemcpyAsync(L->origin.p, E.uq_vals.p, sizeof(u32) * keep, cudaMemcpyDeviceToDevice, E.stream));
     L->count = keep;
@@ -1287,7 +1306,7 @@ void Solver::reduce(const Automaton& A, const sw_reduce_config& cfg, Bounds& b, 
   u64 mlsw = 0;
   bool found = false;
   std::vector<uint32_t> word;
-  DevBuf counts;
+  DevBuf& counts = E.red_counts;
   auto done = [&] {
     st.device_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     E.st = nullptr;
@@ -1664,7 +1683,9 @@ void Solver::learned_beam(const Automaton& A, const sw_learned_beam_config& cfg,
     E.F.vis_count = 0;
   }
   const u32 width = (u32)std::min<uint64_t>(cfg.beam_size, 1u << 26);
-  DevBuf counts, scores, keys, vals, alt_k, alt_v, sel_rows, sel_origin;
+  // engine-owned, kept across calls: freeing device memory would synchronise the device
+  DevBuf &counts = E.lb_counts, &scores = E.lb_scores, &keys = E.lb_keys, &vals = E.lb_vals;
+  DevBuf &alt_k = E.lb_alt_k, &alt_v = E.lb_alt_v, &sel_rows = E.lb_sel_rows, &sel_origin = E.lb_sel_origin;
   std::vector<u32> pc;
   u64 found_len = 0;
   std::vector<uint32_t> word;
