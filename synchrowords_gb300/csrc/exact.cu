@@ -163,7 +163,7 @@ class Engine {
     prof_on = false;
   }
   u32* d_misc = nullptr;  // [0..3] witness, [8] scan total, [kScanErrWord] subset-scan copy timeout
-  static constexpr int kScanErrWord = 60;
+  static constexpr int kScanErrWord = 4;  // read back with the witness, never cleared by it
   // Throws if a subset-check launch reported a tile copy that never arrived
   // (its bounded wait ran out); `w` is the pinned copy of d_misc[kScanErrWord].
   static void check_scan_error(u32 w) {
@@ -316,32 +316,42 @@ class Engine {
     });
     count_launch(1);
     if (st) st->subsets_expanded += N;
-    // sort the children by layer key, then gather the rows in that order
+    // sort the children by layer key
     sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
-    launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
-    launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
-    count_launch(2);
     if (dominance && !self_check && !visited_subsets) {
       // duplicates only: a child is dropped when it equals its predecessor in
-      // the sorted layer or a visited set — one flag pass, one compaction
-      if (X.vis_count) {
-        timed(3, (double)Nc * 8.0 * W, [&] {
-          launch_clear_members(W, X.vis.as<u64>(), X.vis_count, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(),
-                               stream, X.keymap);
-        });
-        count_launch();
-      }
+      // the sorted layer or a visited set — one flag pass over the children in
+      // sort order (rows read through the sort's permutation), one compaction
+      // that gathers the kept rows and writes their origins into the new layer
+      timed(3, (double)Nc * 8.0 * W, [&] {
+        launch_dedup_flags(W, ch_rows.as<u64>(), ch_vals.as<u32>(), keys.as<u64>(), Nc, X.vis.as<u64>(),
+                           X.vis_count, X.keymap, flags_a.as<u32>(), stream);
+      });
+      count_launch();
       X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(Nc, 1));
-      new_vals.reserve(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
-      const u32 f = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc,
-                            X.rows_alt.as<u64>(), new_vals.as<u32>());
+      std::unique_ptr<Layer> L = X.new_layer();
+      L->origin.reserve(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
+      pos.reserve(sizeof(u32) * (size_t)Nc);
+      scan_tmp.reserve(scan_temp_bytes(Nc));
+      u32* total = d_misc + 8;
+      timed(3, (double)Nc * (4 + 4 + 4 + 8.0 * W + 4), [&] {
+        launch_scan(flags_a.as<u32>(), pos.as<u32>(), Nc, total, scan_tmp.p, stream);
+        launch_compact_gather(W, ch_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), pos.as<u32>(), Nc,
+                              X.rows_alt.as<u64>(), L->origin.as<u32>(), stream);
+      });
+      count_launch(2);
+      const u32 f = read_u32(total);
       if (m) X.unique_growth = (double)f / m;
       if (verbose)
         std::fprintf(stderr, "[sw] %s parents=%u children=%u kept=%u (duplicates only) | %.3f ms\n",
                      forward ? "BFS " : "IBFS", m, Nc, f, vclock() - t_step0);
-      finish_layer(X, W, n, m, f);
+      finish_layer(X, W, n, m, f, std::move(L));
       return;
     }
+    // the other reductions work on the rows in sorted order
+    launch_gather_rows(W, ch_rows.as<u64>(), ch_vals.as<u32>(), Nc, sorted_rows.as<u64>(), stream);
+    launch_unique_flags(W, sorted_rows.as<u64>(), Nc, flags_a.as<u32>(), stream);
+    count_launch(2);
     const u32 u = compact(W, sorted_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), Nc, uq_rows.as<u64>(),
                           uq_vals.as<u32>());
     if (m) X.unique_growth = (double)u / m;  // branching before dominance pruning
@@ -410,17 +420,20 @@ class Engine {
     finish_layer(X, W, n, m, f);
   }
 
-  // The kept children (X.rows_alt, origins in new_vals, f of them) become the
-  // new layer of X: recorded for word tracing and merged into the visited list.
-  void finish_layer(Side& X, int W, int n, u32 m, u32 f) {
+  // The kept children (X.rows_alt, f of them) become the new layer of X:
+  // recorded for word tracing and merged into the visited list.  Their origins
+  // are in `L` when given, else in new_vals.
+  void finish_layer(Side& X, int W, int n, u32 m, u32 f, std::unique_ptr<Layer> L = nullptr) {
     std::swap(X.rows.p, X.rows_alt.p);
     std::swap(X.rows.cap, X.rows_alt.cap);
     X.count = f;
     if (st) st->subsets_kept += f;
-    auto L = X.new_layer();
-    L->origin.reserve(sizeof(u32) * std::max<u32>(f, 1));
-    if (f)
-      SW_CUDA(cudaMemcpyAsync(L->origin.p, new_vals.p, sizeof(u32) * f, cudaMemcpyDeviceToDevice, stream));
+    if (!L) {
+      L = X.new_layer();
+      L->origin.reserve(sizeof(u32) * std::max<u32>(f, 1));
+      if (f)
+        SW_CUDA(cudaMemcpyAsync(L->origin.p, new_vals.p, sizeof(u32) * f, cudaMemcpyDeviceToDevice, stream));
+    }
     L->count = f;
     L->parent_count = m;
     X.layers.push_back(std::move(L));
@@ -511,8 +524,7 @@ class Engine {
     SW_CUDA(cudaMemsetAsync(d_misc, 0, 4 * sizeof(u32), stream));
     query(W, kQueryDisjoint, F.rows.as<u64>(), F.count, Q, q, n, nullptr, true);
     if (st) st->meet_pairs += (u64)F.count * q;
-    SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, stream));
-    SW_CUDA(cudaMemcpyAsync(pinned.as<u32>() + 4, d_misc + kScanErrWord, sizeof(u32), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc, 5 * sizeof(u32), cudaMemcpyDeviceToHost, stream));  // witness + error
     SW_CUDA(cudaStreamSynchronize(stream));
     const u32* w = pinned.as<u32>();
     check_scan_error(w[4]);
@@ -799,9 +811,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
     E.query(W, kQueryDisjoint, E.F.rows.as<u64>(), E.F.count, E.B.rows.as<u64>(), E.B.count,
             n, nullptr, true);
     st.meet_pairs += (u64)E.F.count * E.B.count;
-    SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 4 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));
-    SW_CUDA(cudaMemcpyAsync(E.pinned.as<u32>() + 4, E.d_misc + Engine::kScanErrWord, sizeof(u32),
-                            cudaMemcpyDeviceToHost, E.stream));
+    SW_CUDA(cudaMemcpyAsync(E.pinned.p, E.d_misc, 5 * sizeof(u32), cudaMemcpyDeviceToHost, E.stream));  // witness + error
     SW_CUDA(cudaStreamSynchronize(E.stream));
     const auto t_end = std::chrono::steady_clock::now();
     const u32* w = E.pinned.as<u32>();

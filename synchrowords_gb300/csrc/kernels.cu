@@ -976,6 +976,65 @@ void launch_clear_members(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32
   SW_LAUNCH_CHECK();
 }
 
+// Fused duplicate removal over a key-sorted layer, without materialising the
+// sorted rows: position i of the sort holds child vals[i] of C (its layer key
+// keys[2i..2i+1]); flags[i] = 1 when that child differs from child vals[i-1]
+// and equals no row of the key-sorted visited list V.
+template <int W>
+__global__ void k_dedup_flags(const u64* __restrict__ C, const u32* __restrict__ vals, const u64* __restrict__ keys,
+                              u32 m, const u64* __restrict__ V, u32 nv, KeyMap map, u32* __restrict__ flags) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const u64* x = C + (size_t)vals[i] * W;
+  bool keep = i == 0 || !row_eq<W>(x, C + (size_t)vals[i - 1] * W);
+  if (keep && nv) {
+    const u64 x0 = keys[2 * (size_t)i], x1 = keys[2 * (size_t)i + 1];
+    u32 lo = 0, hi = nv;
+    while (lo < hi) {
+      const u32 mid = (lo + hi) >> 1;
+      u64 y0, y1;
+      layer_key<W>(V + (size_t)mid * W, map, y0, y1);
+      if (y0 < x0 || (y0 == x0 && y1 < x1)) lo = mid + 1;
+      else hi = mid;
+    }
+    for (u32 j = lo; j < nv && keep; ++j) {
+      const u64* y = V + (size_t)j * W;
+      u64 y0, y1;
+      layer_key<W>(y, map, y0, y1);
+      if (y0 != x0 || y1 != x1) break;
+      if (row_eq<W>(x, y)) keep = false;
+    }
+  }
+  flags[i] = keep ? 1u : 0u;
+}
+
+// out_rows[pos[i]] = C[vals[i]], out_vals[pos[i]] = vals[i] for the flagged i.
+template <int W>
+__global__ void k_compact_gather(const u64* __restrict__ C, const u32* __restrict__ vals,
+                                 const u32* __restrict__ flags, const u32* __restrict__ pos, u32 m,
+                                 u64* __restrict__ out_rows, u32* __restrict__ out_vals) {
+  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m || !flags[i]) return;
+  const u32 d = pos[i], src = vals[i];
+#pragma unroll
+  for (int w = 0; w < W; ++w) out_rows[(size_t)d * W + w] = C[(size_t)src * W + w];
+  out_vals[d] = src;
+}
+
+void launch_dedup_flags(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
+                        const KeyMap& map, u32* flags, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_dedup_flags<WW><<<(m + 255) / 256, 256, 0, s>>>(C, vals, keys, m, V, nv, map, flags)));
+  SW_LAUNCH_CHECK();
+}
+
+void launch_compact_gather(int W, const u64* C, const u32* vals, const u32* flags, const u32* pos, u32 m,
+                           u64* out_rows, u32* out_vals, cudaStream_t s) {
+  if (!m) return;
+  SW_DISPATCH_W(W, (k_compact_gather<WW><<<(m + 255) / 256, 256, 0, s>>>(C, vals, flags, pos, m, out_rows, out_vals)));
+  SW_LAUNCH_CHECK();
+}
+
 void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
                        const KeyMap& map) {
   if (!nc || !nv) return;

@@ -104,6 +104,14 @@ void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* ou
                       const KeyMap& map = KeyMap{});
 // flags[i] = 1 if row i of C equals a row of V (flags untouched otherwise);
 // V and C sorted by the same layer key.
+// Duplicate removal of a key-sorted layer in one pass: flags[i] = 1 when
+// child vals[i] of C differs from child vals[i-1] and equals no row of the
+// key-sorted visited list V (keys = the children's sorted layer keys).
+void launch_dedup_flags(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
+                        const KeyMap& map, u32* flags, cudaStream_t s);
+// out_rows[pos[i]] = C[vals[i]], out_vals[pos[i]] = vals[i] for the flagged i.
+void launch_compact_gather(int W, const u64* C, const u32* vals, const u32* flags, const u32* pos, u32 m,
+                           u64* out_rows, u32* out_vals, cudaStream_t s);
 void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
                        const KeyMap& map = KeyMap{});
 // flags[i] = 0 where flags[i] = 1 and row i of C equals a row of V (same

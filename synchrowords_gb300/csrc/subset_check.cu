@@ -42,17 +42,19 @@ __host__ __device__ inline u32 n_tiles(u32 m) { return (m + kTileRows - 1) / kTi
 __host__ __device__ inline u32 n_supers(u32 m) { return (m + kSuperRows - 1) / kSuperRows; }
 }  // namespace
 
-// AND masks: tiles first (n_tiles(m) entries), then super-tiles.  One warp
-// per tile: each lane ANDs two rows, a butterfly combines the lanes, and the
-// tile mask is folded into its super-tile's mask (pre-set to all ones).
+// AND masks: tiles first (n_tiles(m) entries), then super-tiles.  One block
+// per super-tile, one warp per tile: each lane ANDs two rows, a butterfly
+// combines the lanes, and warp 0 folds the block's tile masks into the
+// super-tile's mask (so no mask needs presetting and no atomics are used).
 template <int W>
-__global__ void k_range_and(const u64* __restrict__ S, u32 m, u64* __restrict__ masks) {
+__global__ void __launch_bounds__(kTilesPerSuper * 32) k_range_and(const u64* __restrict__ S, u32 m,
+                                                                   u64* __restrict__ masks) {
+  __shared__ u64 s_and[kTilesPerSuper][W];
   const u32 tiles = n_tiles(m);
-  const u32 t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (t >= tiles) return;  // warp-uniform
-  const u32 r0 = t * kTileRows + lane, r1 = r0 + 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32 t = blockIdx.x * kTilesPerSuper + warp;
   u64* super_and = masks + (size_t)tiles * W;
+  const u32 r0 = t * kTileRows + lane, r1 = r0 + 32;
 #pragma unroll
   for (int w = 0; w < W; ++w) {
     u64 a = r0 < m ? S[(size_t)r0 * W + w] : ~0ULL;
@@ -60,9 +62,16 @@ __global__ void k_range_and(const u64* __restrict__ S, u32 m, u64* __restrict__ 
 #pragma unroll
     for (int o = 16; o; o >>= 1) a &= __shfl_xor_sync(kFullMask, a, o);
     if (lane == 0) {
-      masks[(size_t)t * W + w] = a;
-      atomicAnd(&super_and[(size_t)(t / kTilesPerSuper) * W + w], a);
+      if (t < tiles) masks[(size_t)t * W + w] = a;
+      s_and[warp][w] = a;  // ~0 for tiles past the end
     }
+  }
+  __syncthreads();
+  if (warp == 0 && lane < W) {
+    u64 a = ~0ULL;
+#pragma unroll
+    for (int x = 0; x < kTilesPerSuper; ++x) a &= s_and[x][lane];
+    super_and[(size_t)blockIdx.x * W + lane] = a;
   }
 }
 
@@ -267,18 +276,16 @@ size_t subset_check_temp_bytes(int W, u32 m) {
 
 void launch_tile_and(int W, const u64* S, u32 m, u64* masks, cudaStream_t s) {
   if (!m) return;
-  const u32 tiles = n_tiles(m);
-  SW_CUDA(cudaMemsetAsync(masks + (size_t)tiles * W, 0xff, sizeof(u64) * W * n_supers(m), s));
-  const u32 blocks = (tiles * 32 + 255) / 256;
+  const u32 blocks = n_supers(m);
   switch (W) {
-    case 1: k_range_and<1><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 2: k_range_and<2><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 3: k_range_and<3><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 4: k_range_and<4><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 5: k_range_and<5><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 6: k_range_and<6><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 7: k_range_and<7><<<blocks, 256, 0, s>>>(S, m, masks); break;
-    case 8: k_range_and<8><<<blocks, 256, 0, s>>>(S, m, masks); break;
+    case 1: k_range_and<1><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 2: k_range_and<2><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 3: k_range_and<3><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 4: k_range_and<4><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 5: k_range_and<5><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 6: k_range_and<6><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 7: k_range_and<7><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    case 8: k_range_and<8><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
     default: throw std::runtime_error("range_and: unsupported width");
   }
   SW_LAUNCH_CHECK();
