@@ -375,6 +375,16 @@ int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32
                  const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets, const float* labels,
                  uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* loss);
 
+/* sw_mlp_train with a ranking term: groups[j] is a group id per pair (its
+ * BFS layer); the loss adds rank_weight / batch times, over the pairs (a, b)
+ * of one group in a batch with labels[a] < labels[b], log(1 + exp(y_a - y_b)),
+ * so that within a layer a set nearer to a singleton scores lower — the order
+ * a beam keeps.  rank_weight = 0 is plain sw_mlp_train. */
+int sw_mlp_train_ranked(sw_context* ctx, float* params, uint32_t automata, const uint32_t* deltas,
+                        const uint32_t* ns, const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets,
+                        const float* labels, const uint32_t* groups, float rank_weight, uint32_t epochs,
+                        uint32_t batch, float lr, uint64_t seed, float* loss);
+
 /* ---- allocation-free variant --------------------------------------------
  * No counterpart in the reference (its GPU helpers cudaMalloc and cudaFree
  * on every call, preprocessed_transition_kernel.cu:65-87).

@@ -178,6 +178,9 @@ def load_library():
                                    ctypes.c_uint64, _F32P]
     lib.sw_mlp_gradient.argtypes = [ctypes.c_void_p, _F32P, _U32P, ctypes.c_uint32, ctypes.c_uint32, _U64P, _F32P,
                                     ctypes.c_uint64, _F32P, _F32P]
+    lib.sw_mlp_train_ranked.argtypes = [ctypes.c_void_p, _F32P, ctypes.c_uint32, _U32P, _U32P, _U32P, _U64P, _U64P,
+                                        _F32P, _U32P, ctypes.c_float, ctypes.c_uint32, ctypes.c_uint32,
+                                        ctypes.c_float, ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]
     lib.sw_mlp_train.argtypes = [ctypes.c_void_p, _F32P, ctypes.c_uint32, _U32P, _U32P, _U32P, _U64P, _U64P, _F32P,
                                  ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_uint64, _F32P]
     lib.sw_profile_begin.argtypes = [ctypes.c_void_p]
@@ -322,8 +325,11 @@ class Context:
         return g, loss.value
 
     def mlp_train(self, params, automata, sets_per_automaton, labels_per_automaton, epochs: int = 1,
-                  batch: int = 512, lr: float = 1e-3, seed: int = 1) -> Tuple[np.ndarray, float]:
-        """Adam training; returns (trained parameters, mean batch loss of the last epoch)."""
+                  batch: int = 512, lr: float = 1e-3, seed: int = 1, groups_per_automaton=None,
+                  rank_weight: float = 0.0) -> Tuple[np.ndarray, float]:
+        """Adam training; returns (trained parameters, mean batch loss of the last epoch).  With
+        groups (one id per set, e.g. its BFS layer) and rank_weight > 0 the loss adds a pairwise
+        ranking term within each group."""
         p = _f32(params).copy()
         deltas = np.concatenate([_u32(d) for _, _, d in automata])
         ns = _u32([n for n, _, _ in automata])
@@ -334,10 +340,12 @@ class Context:
                                                     for s in sets_per_automaton]), dtype=np.uint64)
         labels = _f32(np.concatenate(labels_per_automaton))
         loss = ctypes.c_float()
-        _check(self._lib.sw_mlp_train(self._h, p.ctypes.data_as(_F32), len(automata), deltas.ctypes.data_as(_U32P),
-                                      ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P), offs.ctypes.data_as(_U64P),
-                                      sets.ctypes.data_as(_U64P), labels.ctypes.data_as(_F32), epochs, batch, lr,
-                                      seed, ctypes.byref(loss)))
+        grp = _u32(np.concatenate(groups_per_automaton)) if groups_per_automaton is not None else None
+        _check(self._lib.sw_mlp_train_ranked(
+            self._h, p.ctypes.data_as(_F32), len(automata), deltas.ctypes.data_as(_U32P), ns.ctypes.data_as(_U32P),
+            ks.ctypes.data_as(_U32P), offs.ctypes.data_as(_U64P), sets.ctypes.data_as(_U64P),
+            labels.ctypes.data_as(_F32), grp.ctypes.data_as(_U32P) if grp is not None else None,
+            rank_weight if grp is not None else 0.0, epochs, batch, lr, seed, ctypes.byref(loss)))
         return p, loss.value
 
     def close(self) -> None:

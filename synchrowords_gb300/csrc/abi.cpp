@@ -875,6 +875,16 @@ int sw_mlp_gradient(sw_context* ctx, const float* params, const uint32_t* delta,
 int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32_t* deltas, const uint32_t* ns,
                  const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets, const float* labels,
                  uint32_t epochs, uint32_t batch, float lr, uint64_t seed, float* loss) {
+  return sw_mlp_train_ranked(ctx, params, automata, deltas, ns, ks, offsets, sets, labels, nullptr, 0.0f, epochs,
+                             batch, lr, seed, loss);
+}
+
+int sw_mlp_train_ranked(sw_context* ctx, float* params, uint32_t automata, const uint32_t* deltas,
+                        const uint32_t* ns, const uint32_t* ks, const uint64_t* offsets, const uint64_t* sets,
+                        const float* labels, const uint32_t* groups, float rank_weight, uint32_t epochs,
+                        uint32_t batch, float lr, uint64_t seed, float* loss) {
+  if (rank_weight < 0.0f || (rank_weight > 0.0f && !groups))
+    return fail(SW_ERR_INVALID_ARGUMENT, "a ranking weight needs a group per pair");
   if (!ctx || !params || !deltas || !ns || !ks || !offsets || !sets || !labels || !loss)
     return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
   return guarded([&] {
@@ -886,7 +896,7 @@ int sw_mlp_train(sw_context* ctx, float* params, uint32_t automata, const uint32
       if (offsets[i + 1] < offsets[i]) throw std::invalid_argument("pair offsets must not decrease");
     }
     ctx->solver->set_model(params);
-    *loss = ctx->solver->mlp_train(autos, offsets, sets, labels, epochs, batch, lr, seed);
+    *loss = ctx->solver->mlp_train(autos, offsets, sets, labels, epochs, batch, lr, seed, groups, rank_weight);
     ctx->solver->get_model(params);
     return SW_OK;
   });

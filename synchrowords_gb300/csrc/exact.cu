@@ -1613,7 +1613,8 @@ float Solver::mlp_gradient(const Automaton& A, const uint64_t* sets, const float
 }
 
 float Solver::mlp_train(const std::vector<Automaton>& autos, const uint64_t* offsets, const uint64_t* sets,
-                        const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed) {
+                        const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                        const uint32_t* groups, float rank_w) {
   SW_CUDA(cudaSetDevice(device_));
   Engine& E = *eng_;
   const size_t A_n = autos.size();
@@ -1631,6 +1632,11 @@ float Solver::mlp_train(const std::vector<Automaton>& autos, const uint64_t* off
     SW_CUDA(cudaMemcpy(d_rows.as<u64>() + o * 8, rows.data(), sizeof(u64) * rows.size(), cudaMemcpyHostToDevice));
   }
   SW_CUDA(cudaMemcpy(d_lab.p, labels, sizeof(float) * total, cudaMemcpyHostToDevice));
+  DevBuf d_grp;
+  if (groups && rank_w > 0.0f) {
+    d_grp.reserve(sizeof(uint32_t) * total);
+    SW_CUDA(cudaMemcpy(d_grp.p, groups, sizeof(uint32_t) * total, cudaMemcpyHostToDevice));
+  }
   std::vector<size_t> order(A_n);
   for (size_t a = 0; a < A_n; ++a) order[a] = a;
   uint64_t state = seed;
@@ -1652,7 +1658,7 @@ float Solver::mlp_train(const std::vector<Automaton>& autos, const uint64_t* off
         E.mlp->prepare(autos[a]);
         E.mlp->zero_grad();
         E.mlp->forward(d_rows.as<u64>() + o * 8, 8, c, d_y.as<float>());
-        E.mlp->backward(d_lab.as<float>() + o, c);
+        E.mlp->backward(d_lab.as<float>() + o, c, d_grp.p ? d_grp.as<uint32_t>() + o : nullptr, rank_w);
         E.mlp->adam_step(lr);
         float l = 0;
         SW_CUDA(cudaMemcpyAsync(&l, E.mlp->loss(), sizeof(float), cudaMemcpyDeviceToHost, E.stream));

@@ -66,8 +66,11 @@ class Solver {
                           std::vector<uint64_t>& sets, std::vector<float>& labels, std::vector<uint32_t>& depths);
   void mlp_forward(const Automaton& A, const uint64_t* sets, uint64_t count, float* out);
   float mlp_gradient(const Automaton& A, const uint64_t* sets, const float* labels, uint64_t count, float* grad);
+  // groups (optional): a group id per pair; with rank_w > 0 the loss adds a
+  // pairwise ranking term within each group of a batch.
   float mlp_train(const std::vector<Automaton>& autos, const uint64_t* offsets, const uint64_t* sets,
-                  const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed);
+                  const float* labels, uint32_t epochs, uint32_t batch, float lr, uint64_t seed,
+                  const uint32_t* groups = nullptr, float rank_w = 0.0f);
 
   // Kernel-level helpers (reference bitset layout on the host).
   void apply_transition(const Automaton& A, uint32_t letter, bool inverse, const uint64_t* from, uint64_t* to,

@@ -105,7 +105,7 @@ void MlpRunner::zero_grad() {
   SW_CUDA(cudaMemsetAsync(loss_.p, 0, sizeof(float), stream_));
 }
 
-void MlpRunner::backward(const float* t, u32 count) {
+void MlpRunner::backward(const float* t, u32 count, const uint32_t* grp, float rank_w) {
   if (!count || count != count_) throw std::runtime_error("backward: batch differs from the forward batch");
   const size_t c = count;
   dy_.reserve(sizeof(float) * c * 2);
@@ -124,6 +124,7 @@ void MlpRunner::backward(const float* t, u32 count) {
   float* yy = dy_.as<float>() + c;
   mlp::head(h2b_.as<bf16>(), params_.as<float>(), B, yy, stream_);
   mlp::mse(yy, t, B, dy_.as<float>(), loss_.as<float>(), stream_);
+  if (grp && rank_w > 0.0f) mlp::rank_add(yy, t, grp, B, rank_w, dy_.as<float>(), loss_.as<float>(), stream_);
   // head: dw3, db3, dH2 = dy w3^T * [h2 > 0]
   mlp::head_back(dy_.as<float>(), h2b_.as<bf16>(), h2_.as<float>(), params_.as<float>(), B, g, dh2_.as<float>(),
                  dh2b_.as<bf16>(), stream_);

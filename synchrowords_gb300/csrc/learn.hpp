@@ -29,7 +29,9 @@ class MlpRunner {
 
   // After forward() on the same rows: gradient of the mean squared error
   // against targets t (device) added into grad(); loss added into loss().
-  void backward(const float* t, u32 count);
+  // With `grp` (a group id per row, e.g. its BFS layer) and rank_w > 0 the
+  // loss adds rank_w times a pairwise ranking term within each group.
+  void backward(const float* t, u32 count, const uint32_t* grp = nullptr, float rank_w = 0.0f);
 
   void zero_grad();
   void adam_step(float lr);  // then refreshes the bf16 weight copies

@@ -320,6 +320,50 @@ void mse(const float* y, const float* t, int rows, float* dy, float* loss, cudaS
   SW_LAUNCH_CHECK();
 }
 
+// Pairwise ranking term over the rows of one group (one BFS layer): for every
+// pair with t_a < t_b, w / rows * softplus(y_a - y_b), so that a set nearer to
+// a singleton scores lower than its sibling; its gradient is added to dy.
+__global__ void k_rank_add(const float* __restrict__ y, const float* __restrict__ tgt, const uint32_t* __restrict__ grp,
+                           int rows, float w, float* dy, float* loss) {
+  __shared__ float s_sum[8];
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float l = 0.0f;
+  if (i < rows) {
+    const float yi = y[i], ti = tgt[i];
+    const uint32_t gi = grp[i];
+    float g = 0.0f;
+    for (int j = 0; j < rows; ++j) {
+      if (grp[j] != gi) continue;
+      const float tj = tgt[j];
+      if (ti < tj) {  // i should score below j
+        const float z = yi - y[j];
+        g += 1.0f / (1.0f + __expf(-z));
+        l += z > 20.0f ? z : log1pf(__expf(z));
+      } else if (tj < ti) {  // j should score below i
+        g -= 1.0f / (1.0f + __expf(-(y[j] - yi)));
+      }
+    }
+    dy[i] += w * g / (float)rows;
+    l *= w / (float)rows;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0) s_sum[threadIdx.x >> 5] = l;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.0f;
+    for (int x = 0; x < (int)(blockDim.x >> 5); ++x) b += s_sum[x];
+    atomicAdd(loss, b);
+  }
+}
+
+void rank_add(const float* y, const float* t, const uint32_t* grp, int rows, float w, float* dy, float* loss,
+              cudaStream_t s) {
+  if (!rows || w == 0.0f) return;
+  k_rank_add<<<(rows + 255) / 256, 256, 0, s>>>(y, t, grp, rows, w, dy, loss);
+  SW_LAUNCH_CHECK();
+}
+
 // block of 128 threads = one hidden column each; rows in chunks
 __global__ void k_head_back(const float* __restrict__ dy, const __nv_bfloat16* __restrict__ H,
                             const float* __restrict__ pre, const float* __restrict__ params, int rows, int rows_per_block,

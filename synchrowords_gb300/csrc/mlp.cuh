@@ -57,6 +57,10 @@ void head(const __nv_bfloat16* H, const float* params, int rows, float* y, cudaS
 
 // Loss 1/B sum (y - t)^2 (loss[0] += ...) and dy = 2 (y - t) / B.
 void mse(const float* y, const float* t, int rows, float* dy, float* loss, cudaStream_t s);
+// Adds w/B sum over pairs of one group with t_a < t_b of softplus(y_a - y_b)
+// to the loss and its gradient to dy (a within-layer ranking term).
+void rank_add(const float* y, const float* t, const uint32_t* grp, int rows, float w, float* dy, float* loss,
+              cudaStream_t s);
 
 // From dy: grad of w3 and b3 (grad vector, accumulated), and the masked
 // hidden gradient dH = dy w3^T * [pre > 0] (fp32 and bf16).

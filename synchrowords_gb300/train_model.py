@@ -11,7 +11,9 @@ uniform in [--n-min, --n-max], k = 2, SplitMix64 seeds from --seed.
 The target is the merge length itself; `--relative 1` trains on the merge
 length minus the mean over its layer instead (the differences a beam ranks
 by; measured worse: per-layer rank correlation 0.28 against 0.51 for set
-size).  A held-out share is scored after training: mean squared error, and
+size).  `--rank-weight W` adds a pairwise ranking term within each layer
+(sw_mlp_train_ranked): for siblings with merge lengths a < b,
+W * log(1 + exp(y_a - y_b)).  A held-out share is scored after training: mean squared error, and
 per layer the rank correlation of predictions with the labels beside the
 same correlation for set size (the plain beam's key).
 """
@@ -64,6 +66,8 @@ def main() -> None:
     ap.add_argument("--out", default=str(DEFAULT_MODEL))
     ap.add_argument("--report", default="")
     ap.add_argument("--relative", type=int, default=0, help="train on merge length minus the layer mean")
+    ap.add_argument("--rank-weight", type=float, default=0.0,
+                    help="add a pairwise ranking term within each BFS layer, with this weight")
     a = ap.parse_args()
 
     g = splitmix64(a.seed)
@@ -91,7 +95,9 @@ def main() -> None:
     params = init_params(np.random.default_rng(a.seed), mean)
     t1 = time.time()
     params, loss = ctx.mlp_train(params, [x[0] for x in train], [x[1] for x in train], [x[2] for x in train],
-                                 epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed)
+                                 epochs=a.epochs, batch=a.batch, lr=a.lr, seed=a.seed,
+                                 groups_per_automaton=[x[3] for x in train] if a.rank_weight > 0 else None,
+                                 rank_weight=a.rank_weight)
     t_train = time.time() - t1
     mse, mse_mean, rho, rho_size = [], [], [], []
     for (n, k, d), sets, target, depths in test:
