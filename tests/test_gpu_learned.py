@@ -158,29 +158,39 @@ def test_size_ordered_beam_without_a_model(ctx):
 
 
 def test_what_the_trained_network_gains(ctx):
-    """The same forward beam (width 4096) on held-out random binary DFAs
-    (n = 200), ranked by the trained network, by the same network untrained
-    (its initial weights), and by set size (the beam without a network).
-    Training must pay: the trained network's bounds are closer to the exact
-    lengths than the untrained one's.  The size-ranked beam is measured beside
-    them (on these automata it is as good or better: the ranking the network
-    learns is no sharper than size within a layer)."""
+    """What the trained network gains over the method without it.  The same
+    forward beam (width 4096) ranks each layer's children by the packaged
+    network (trained with a within-layer ranking term), by set size (the beam
+    without a network) and by the same network untrained.  Measured on 12
+    held-out random binary DFAs (n = 200) as the summed gap between the bound
+    and the exact length, and on the sixteen n = 320 / 384 bench automata as
+    the summed bound (the reference's dynamic Beam, width up to n^2 log2 n,
+    reaches the exact length on every one of those: sums 360 / 397).  The
+    trained network's bounds must be closer to the exact lengths than the
+    size-ranked beam's over both sets, and than its own untrained start's."""
     if not sw.DEFAULT_MODEL.exists():
         pytest.skip("no packaged model")
     untrained = sw.Context(0, model=None)
     untrained.set_model(init_params(np.random.default_rng(7), 16.0))
     try:
-        gaps = {"trained": [], "untrained": [], "size": []}
+        gaps = {"trained": 0, "untrained": 0, "size": 0}
         for i in range(12):
             n = 200
             d = random_dfa(n, 2, 880000 + i)
             exact = ctx.solve(d, n, 2, plan(("Exact", {}))).upper
-            gaps["trained"].append(ctx.solve(d, n, 2, plan(("LearnedBeam", {"order": "model"}))).upper - exact)
-            gaps["untrained"].append(
-                untrained.solve(d, n, 2, plan(("LearnedBeam", {"order": "model"}))).upper - exact)
-            gaps["size"].append(ctx.solve(d, n, 2, plan(("LearnedBeam", {"order": "size"}))).upper - exact)
-        print("gap to exact:", gaps)
-        assert all(min(g) >= 0 for g in gaps.values())
-        assert sum(gaps["trained"]) < sum(gaps["untrained"])
+            for name, c, order in (("trained", ctx, "model"), ("untrained", untrained, "model"), ("size", ctx, "size")):
+                bound = c.solve(d, n, 2, plan(("LearnedBeam", {"order": order}))).upper
+                assert bound >= exact
+                gaps[name] += bound - exact
+        bench = {"trained": 0, "size": 0}
+        for n, exact_sum in ((320, 360), (384, 397)):
+            for name, order in (("trained", "model"), ("size", "size")):
+                s = sum(ctx.solve(random_dfa(n, 2, seed), n, 2, plan(("LearnedBeam", {"order": order}))).upper
+                        for seed in range(1, 9))
+                assert s >= exact_sum
+                bench[name] += s
+        print("bound gap to exact (n = 200):", gaps, "bound sums (n = 320 + 384):", bench)
+        assert gaps["trained"] < gaps["untrained"]
+        assert gaps["trained"] + bench["trained"] < gaps["size"] + bench["size"]
     finally:
         untrained.close()
