@@ -113,8 +113,20 @@ def test_training_lowers_the_loss(ctx):
     _, loss0 = ctx.mlp_gradient(p0, autos[0][2], autos[0][0], 2, S[0], L[0])
     p1, loss_last = ctx.mlp_train(p0, autos, S, L, epochs=40, batch=256, lr=1e-3, seed=3)
     _, loss1 = ctx.mlp_gradient(p1, autos[0][2], autos[0][0], 2, S[0], L[0])
+    # training loads its result into the context: give the shared context its packaged model back
+    if sw.DEFAULT_MODEL.exists():
+        ctx.set_model(sw.load_model())
     assert np.isfinite(loss_last)
     assert loss1 < 0.8 * loss0, (loss0, loss1)
+    # the ranking term trains too, and a weight without groups is refused
+    groups = [np.zeros(len(x), dtype=np.uint32) for x in L]
+    c = sw.Context(0, model=None)
+    try:
+        p2, loss2 = c.mlp_train(p0, autos, S, L, epochs=5, batch=256, lr=1e-3, seed=3, groups_per_automaton=groups,
+                                rank_weight=1.0)
+        assert np.isfinite(loss2) and not np.array_equal(p2, p0)
+    finally:
+        c.close()
 
 
 def plan(*algos):
@@ -157,7 +169,7 @@ def test_size_ordered_beam_without_a_model(ctx):
         c.close()
 
 
-def test_what_the_trained_network_gains(ctx):
+def test_what_the_trained_network_gains():
     """What the trained network gains over the method without it.  The same
     forward beam (width 4096) ranks each layer's children by the packaged
     network (trained with a within-layer ranking term), by set size (the beam
@@ -170,6 +182,7 @@ def test_what_the_trained_network_gains(ctx):
     size-ranked beam's over both sets, and than its own untrained start's."""
     if not sw.DEFAULT_MODEL.exists():
         pytest.skip("no packaged model")
+    ctx = sw.Context(0)  # the packaged model, whatever earlier tests loaded elsewhere
     untrained = sw.Context(0, model=None)
     untrained.set_model(init_params(np.random.default_rng(7), 16.0))
     try:
@@ -194,3 +207,4 @@ def test_what_the_trained_network_gains(ctx):
         assert gaps["trained"] + bench["trained"] < gaps["size"] + bench["size"]
     finally:
         untrained.close()
+        ctx.close()
