@@ -56,6 +56,9 @@ def test_batch_entry_points_reject_null_arguments(native_lib):
     assert lib.sw_solve_batch(None, 1, None, None, None, b"{}", None, 0) == -1
     assert lib.sw_autotune_batch(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
     assert lib.sw_autotune_cluster(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
+    assert lib.sw_batch_last_profile(None, None) == -1
+    assert lib.sw_mlp_train_ranked(None, None, 0, None, None, None, None, None, None, None, 0.0, 1, 1, 0.0, 0,
+                                   None) == -1
     assert b"NULL" in lib.sw_last_error()
 
 
@@ -275,7 +278,19 @@ def test_learned_beam_plan_entry(native_lib):
         assert d["algorithms"][0]["order"] == code
 
 
+def test_exact_reductions_key(native_lib):
+    """The Exact entry's own "reductions" key (auto by default)."""
+    d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "Exact"}]}), 200, 2)["algorithms"][0]
+    assert d["reductions"] == 0
+    for value, code in (("auto", 0), ("always", 1), ("memory", 2)):
+        cfg = {"reductions": value}
+        d = sw.plan_from_json(json.dumps({"algorithms": [{"name": "Exact", "config": cfg}]}), 200, 2)
+        assert d["algorithms"][0]["reductions"] == code
+
+
 @pytest.mark.parametrize("bad", [
+    '{"algorithms": [{"name": "Exact", "config": {"reductions": "never"}}]}',
+    '{"algorithms": [{"name": "Exact", "config": {"reductions": 1}}]}',
     '{"algorithms": []}', '{"algorithms": [{"name": "Nope", "config": {}}]}', '{"threads": 0, "algorithms": '
     '[{"name": "Exact", "config": {}}]}', '{"threads": 65, "algorithms": [{"name": "Exact"}]}',
     '{"algorithms": [{"name": "Beam", "config": {"presort": "outdeg"}}]}', '{"algorithms": [', 'null',
