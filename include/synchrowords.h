@@ -253,6 +253,8 @@ typedef struct {
   uint64_t children;        /* children expanded by the cluster launches */
   uint64_t staged_bytes;    /* backward rows the cluster launches' meet checks staged (bit-sliced) on chip */
   uint64_t steps;           /* BFS levels of the cluster launches */
+  uint32_t graph_replays;   /* device rounds replayed from a CUDA graph captured for an earlier batch of the same
+                               shape (each round's launches are captured once per shape and buffer set) */
 } sw_batch_profile;
 
 int sw_batch_last_profile(sw_context* ctx, sw_batch_profile* out);

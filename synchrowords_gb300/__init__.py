@@ -111,7 +111,7 @@ class _BatchProfile(ctypes.Structure):
     _fields_ = [("small_solved", ctypes.c_uint32), ("cluster_solved", ctypes.c_uint32),
                 ("streamed", ctypes.c_uint32), ("launches", ctypes.c_uint32), ("device_ms", ctypes.c_double),
                 ("meet_pairs", ctypes.c_uint64), ("children", ctypes.c_uint64), ("staged_bytes", ctypes.c_uint64),
-                ("steps", ctypes.c_uint64)]
+                ("steps", ctypes.c_uint64), ("graph_replays", ctypes.c_uint32)]
 
 
 class _KernelProfile(ctypes.Structure):

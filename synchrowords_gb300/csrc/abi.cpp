@@ -32,7 +32,12 @@ struct SmallBatchState {
   size_t c_zeroed = 0;       // bytes of c_scratch zero-filled since its allocation
   uint64_t c_tags_used = 0;  // upper bound on the tags taken since the last zero fill
   sw_batch_profile last{};
+  // CUDA graphs of recent device rounds, keyed by everything their launches
+  // bake in (buffers, per-width counts, cluster geometry): a batch of a shape
+  // seen before replays its round with one graph launch
+  std::vector<std::pair<std::vector<uint64_t>, cudaGraphExec_t>> graphs;
   ~SmallBatchState() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -239,6 +244,7 @@ struct DeviceRound {
   int launches = 0;
   uint32_t word_stride = 1024;
   bool active = false;
+  bool replayed = false;  // launched from a graph captured for an earlier batch of the same shape
 };
 
 void start_round(sw_context* ctx, DeviceRound& D, const std::vector<uint32_t> small[4],
@@ -310,7 +316,6 @@ void start_round(sw_context* ctx, DeviceRound& D, const std::vector<uint32_t> sm
     }
     S.c_tags_used += tags;
     S.c_stats.reserve(sizeof(uint64_t) * 9);
-    SW_CUDA(cudaMemsetAsync(S.c_stats.p, 0, sizeof(uint64_t) * 9, S.stream));
   }
   SW_CUDA(cudaMemcpyAsync(S.inst.p, inst.data(), sizeof(sw::SmallInstance) * inst.size(), cudaMemcpyHostToDevice,
                           S.stream));
@@ -318,23 +323,64 @@ void start_round(sw_context* ctx, DeviceRound& D, const std::vector<uint32_t> sm
   SW_CUDA(cudaMemcpyAsync(S.seeds.p, spool.data(), spool.size(), cudaMemcpyHostToDevice, S.stream));
   SW_CUDA(cudaEventCreate(&D.t0));
   SW_CUDA(cudaEventCreate(&D.t1));
-  SW_CUDA(cudaEventRecord(D.t0, S.stream));
-  for (int c = 0; c < 8; ++c) {
-    const size_t a = class_start[c], b = class_start[c + 1];
-    if (a == b) continue;
-    ++D.launches;
-    const int W = c % 4 + 1;
-    if (c < 4)
-      sw::launch_small_batch(W, S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a), S.delta.as<uint8_t>(),
-                             S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
-                             S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.origins.as<uint32_t>(),
-                             S.visited.as<sw::u64>(), blocks, S.counter.as<uint32_t>(), S.stream);
-    else
-      sw::launch_cluster_batch(W, cs, clusters[c - 4], S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a),
-                               S.delta.as<uint8_t>(), S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
-                               S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.c_scratch.p, caps,
-                               S.counter.as<uint32_t>(), S.c_stats.as<sw::u64>(), S.stream);
+  // the round's device work: the cluster statistics reset and one persistent
+  // launch per non-empty class
+  auto issue = [&] {
+    if (max_clusters) SW_CUDA(cudaMemsetAsync(S.c_stats.p, 0, sizeof(uint64_t) * 9, S.stream));
+    for (int c = 0; c < 8; ++c) {
+      const size_t a = class_start[c], b = class_start[c + 1];
+      if (a == b) continue;
+      const int W = c % 4 + 1;
+      if (c < 4)
+        sw::launch_small_batch(W, S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a), S.delta.as<uint8_t>(),
+                               S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
+                               S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.origins.as<uint32_t>(),
+                               S.visited.as<sw::u64>(), blocks, S.counter.as<uint32_t>(), S.stream);
+      else
+        sw::launch_cluster_batch(W, cs, clusters[c - 4], S.inst.as<sw::SmallInstance>() + a, (uint32_t)(b - a),
+                                 S.delta.as<uint8_t>(), S.seeds.as<uint8_t>(), S.results.as<sw::SmallResult>() + a,
+                                 S.words.as<uint8_t>() + a * D.word_stride, D.word_stride, S.c_scratch.p, caps,
+                                 S.counter.as<uint32_t>(), S.c_stats.as<sw::u64>(), S.stream);
+    }
+  };
+  for (int c = 0; c < 8; ++c) D.launches += class_start[c] != class_start[c + 1];
+  std::vector<uint64_t> key{(uint64_t)cs, blocks, D.word_stride, (uint64_t)(uintptr_t)S.inst.p,
+                            (uint64_t)(uintptr_t)S.delta.p, (uint64_t)(uintptr_t)S.seeds.p,
+                            (uint64_t)(uintptr_t)S.results.p, (uint64_t)(uintptr_t)S.words.p,
+                            (uint64_t)(uintptr_t)S.origins.p, (uint64_t)(uintptr_t)S.visited.p,
+                            (uint64_t)(uintptr_t)S.counter.p, (uint64_t)(uintptr_t)S.c_scratch.p,
+                            (uint64_t)(uintptr_t)S.c_stats.p};
+  for (int c = 0; c < 9; ++c) key.push_back(class_start[c]);
+  for (int c = 0; c < 4; ++c) key.push_back(clusters[c]);
+  cudaGraphExec_t exec = nullptr;
+  for (auto& g : S.graphs)
+    if (g.first == key) exec = g.second;
+  if (!exec) {
+    // the kernels' attributes are set before the capture (not a stream operation)
+    sw::small_batch_prepare();
+    cudaGraph_t graph = nullptr;
+    SW_CUDA(cudaStreamBeginCapture(S.stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      issue();
+    } catch (...) {
+      cudaStreamEndCapture(S.stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    SW_CUDA(cudaStreamEndCapture(S.stream, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    SW_CUDA(e);
+    if (S.graphs.size() >= 4) {  // keep the four most recent shapes
+      cudaGraphExecDestroy(S.graphs.front().second);
+      S.graphs.erase(S.graphs.begin());
+    }
+    S.graphs.emplace_back(std::move(key), exec);
+  } else {
+    D.replayed = true;
   }
+  SW_CUDA(cudaEventRecord(D.t0, S.stream));
+  SW_CUDA(cudaGraphLaunch(exec, S.stream));
   SW_CUDA(cudaEventRecord(D.t1, S.stream));
   D.active = true;
 }
@@ -366,6 +412,7 @@ std::vector<uint32_t> finish_round(sw_context* ctx, DeviceRound& D, const uint32
   sw_batch_profile& P = S.last;
   P.device_ms += ms;
   P.launches += (uint32_t)D.launches;
+  P.graph_replays += D.replayed ? 1u : 0u;
   P.meet_pairs += cst[0];
   P.children += cst[1];
   P.staged_bytes += cst[2];

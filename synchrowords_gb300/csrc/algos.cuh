@@ -64,6 +64,9 @@ struct SmallResult {
 };
 
 int small_batch_blocks();
+// Raises the shared-memory limits of the batched kernels on the current
+// device (done before a launch is captured into a CUDA graph).
+void small_batch_prepare();
 size_t small_batch_origin_words(int W, u32 blocks);
 size_t small_batch_visited_words(int W, u32 blocks);
 // One persistent launch of `blocks` blocks over `count` automata of set width

@@ -37,6 +37,7 @@
 // IBFS steps (:179-344) and goal check (:90).
 #include <algorithm>
 #include <mutex>
+#include <set>
 #include <utility>
 
 #include "algos.cuh"
@@ -600,11 +601,19 @@ const void* cluster_fn_w(int W) {
 size_t col_smem(int W) { return sizeof(u32) * 64 * (size_t)W * kCtGroups; }
 
 std::mutex g_cluster_mu;
+std::set<std::pair<int, const void*>> g_nonportable;  // (device, kernel) pairs opted in to clusters above 8
 
+// Sets the kernel's attributes once per device, so that a launch issued
+// while a stream is being captured makes no attribute call.
 void prepare(const void* fn, int W, int cs) {
   std::lock_guard<std::mutex> g(g_cluster_mu);
   ensure_smem_limit(fn, (int)col_smem(W));
-  if (cs > 8) SW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  if (cs > 8) {
+    int dev = 0;
+    SW_CUDA(cudaGetDevice(&dev));
+    if (g_nonportable.insert({dev, fn}).second)
+      SW_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  }
 }
 }  // namespace
 

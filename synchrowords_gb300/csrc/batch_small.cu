@@ -357,15 +357,19 @@ size_t small_batch_visited_words(int W, u32 blocks) { return (size_t)blocks * 4 
 
 int small_batch_blocks() { return device_sm_count(); }
 
+void small_batch_prepare() {
+  ensure_smem_limit((const void*)k_small_batch<1>, (int)SmCaps<1>::smem);
+  ensure_smem_limit((const void*)k_small_batch<2>, (int)SmCaps<2>::smem);
+  ensure_smem_limit((const void*)k_small_batch<3>, (int)SmCaps<3>::smem);
+  ensure_smem_limit((const void*)k_small_batch<4>, (int)SmCaps<4>::smem);
+}
+
 void launch_small_batch(int W, const SmallInstance* inst, u32 count, const uint8_t* delta_pool,
                         const uint8_t* seed_pool, SmallResult* results, uint8_t* words, u32 word_stride, u32* origins,
                         u64* visited, u32 blocks, u32* counter, cudaStream_t s) {
   if (!count) return;
   SW_CUDA(cudaMemsetAsync(counter, 0, sizeof(u32), s));
-  ensure_smem_limit((const void*)k_small_batch<1>, (int)SmCaps<1>::smem);
-  ensure_smem_limit((const void*)k_small_batch<2>, (int)SmCaps<2>::smem);
-  ensure_smem_limit((const void*)k_small_batch<3>, (int)SmCaps<3>::smem);
-  ensure_smem_limit((const void*)k_small_batch<4>, (int)SmCaps<4>::smem);
+  small_batch_prepare();
 #define SW_SMALL(WW)                                                                                              \
   k_small_batch<WW><<<blocks, kSmThreads, SmCaps<WW>::smem, s>>>(inst, count, delta_pool, seed_pool, results, words, \
                                                                  word_stride, origins, visited, counter)

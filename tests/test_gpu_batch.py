@@ -73,3 +73,30 @@ def test_autotune_batch_picks_candidates_and_keeps_results(native_lib):
     assert ctx.get_batch_tuning()["cluster_size"] == tuned["cluster_size"]
     check_against_golden(autos, ctx.solve_batch(autos, PLAN))
     ctx.close()
+
+
+def test_repeated_batch_replays_its_captured_round(native_lib):
+    """A batch of a shape seen before replays the device round captured into a
+    CUDA graph for it; a batch of another shape captures its own; answers stay
+    those of the golden file."""
+    import synchrowords_gb300 as sw
+    ctx = sw.Context(0)
+    try:
+        autos = gen.batch(GOLD["count"], GOLD["seed"])[:300]
+        first = ctx.solve_batch(autos, PLAN, workers=4)
+        p1 = ctx.last_batch_profile()
+        assert p1["graph_replays"] == 0 and p1["small_solved"] > 0 and p1["cluster_solved"] > 0, p1
+        check_against_golden(autos, first)
+        again = ctx.solve_batch(autos, PLAN, workers=4)
+        p2 = ctx.last_batch_profile()
+        assert p2["graph_replays"] >= 1 and p2["launches"] == p1["launches"], (p1, p2)
+        # which shortest word a persistent launch finds first may vary between runs; lengths may not
+        assert [(r.lower, r.upper) for r in again] == [(r.lower, r.upper) for r in first]
+        check_against_golden(autos, again)
+        other = autos[:120]
+        check_against_golden(other, ctx.solve_batch(other, PLAN, workers=4))
+        assert ctx.last_batch_profile()["graph_replays"] == 0
+        check_against_golden(autos, ctx.solve_batch(autos, PLAN, workers=4))
+        assert ctx.last_batch_profile()["graph_replays"] >= 1
+    finally:
+        ctx.close()
