@@ -84,9 +84,15 @@ def plan_name(plan: str) -> str:
             PLAN_PLAIN_EXACT: "Exact (configs/exact.json entry)", PLAN_LEARNED_EXACT: "LearnedBeam+Exact"}[plan]
 
 
-def workload_dfas(name: str, rank: int):
+def workload_dfas(name: str, rank: int, held_out: int = 0):
+    """The workload's automata for this rank; with held_out > 0, that many
+    other automata of the same shape (seeds no rank's workload uses)."""
     from synchrowords_gb300.generate import batch, random_dfa
     n, k, count, _, _ = WORKLOADS[name]
+    if held_out:
+        if n == 0:
+            return batch(held_out, 90210 + rank)
+        return [(n, k, random_dfa(n, k, 50000 + rank * 100000 + i)) for i in range(held_out)]
     if n == 0:
         return batch(count, 2026 + rank)
     base = 1 + rank * 100000
@@ -276,7 +282,10 @@ def run_ours(args, world, rank, local):
     stream = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
-    tuned = tuned_c = None
+    tuned = tuned_c = tuned_scan = None
+    if args.scan_tune:
+        # untimed: the subset check's launch shape tuned on held-out automata of the same shape
+        tuned_scan = ctx.autotune_scan(workload_dfas(args.workload, rank, args.scan_tune), plan)
     if args.autotune:
         tuned = ctx.autotune_batch(dfas, plan)  # untimed; keeps the fastest tuning on ctx
         tuned_c = ctx.autotune_cluster(dfas, plan)
@@ -369,6 +378,9 @@ def run_ours(args, world, rank, local):
                    "streams": args.streams if not args.autotune else ctx.get_batch_tuning()["workers"],
                    "batch_tuning": dict(ctx.get_batch_tuning(), autotune_ms=tuned["ms"] if tuned else None,
                                         cluster_autotune_ms=tuned_c["ms"] if tuned_c else None),
+                   "scan_shapes": ({"tuned_on": f"{args.scan_tune} held-out automata of the same shape",
+                                    "keys": tuned_scan} if tuned_scan is not None else
+                                   {"tuned_on": None, "default": sw.DEFAULT_SCAN_SHAPE}),
                    "routes": {k: v for k, v in ctx.last_batch_profile().items()
                               if k in ("small_solved", "cluster_solved", "streamed")},
                    "batched_launch_ms_per_step": round(batched_ms / args.steps, 3),
@@ -404,6 +416,9 @@ def main():
     ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
     ap.add_argument("--autotune", action="store_true",
                     help="before the warm-up, tune the batch's worker count and batched-launch limit on the workload")
+    ap.add_argument("--scan-tune", type=int, default=0, metavar="N",
+                    help="before the warm-up, tune the subset check's launch shape on N held-out automata of the "
+                         "workload's shape (0 = the default shape)")
     ap.add_argument("--learned-vs-plain", type=int, default=0, metavar="N",
                     help="also solve the first N n=384 automata plainly (12 GB and GPU-sized budgets) and with the "
                          "learned bound, and report their wall times (minutes per automaton; off by default)")

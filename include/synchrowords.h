@@ -288,6 +288,52 @@ int sw_autotune_cluster(sw_context* ctx, uint32_t count, const uint32_t* deltas,
                         const double* limit_candidates, uint32_t n_limits, uint32_t reps, double* ms,
                         sw_batch_tuning* best);
 
+/* ---- subset-check launch shape and its autotuner -----------------------
+ * No counterpart in the reference (its trie walk has no launch shape).  The
+ * subset check (sw_subsets_check and every check inside the searches) cuts
+ * the sorted list S into tiles of tile_rows rows with an AND mask per tile and
+ * per super-tile of tiles_per_super tiles; a block of `warps` warps tests 32
+ * queries per warp against the tiles of one chunk of S, and S is chunked so
+ * that the grid holds about grid_factor blocks per SM.  A context keeps one
+ * shape per row width (words = ceil(n / 64), 1..8) and list size class; the
+ * shape changes speed only, never results. */
+typedef struct {
+  int32_t tile_rows;        /* rows of S per tile staged in shared memory: 32, 64 or 128 (default 64) */
+  int32_t warps;            /* warps of 32 queries per block: 4, 8 or 16 (default 8) */
+  int32_t tiles_per_super;  /* tiles per super-tile AND mask: 4, 8, 16 or 32 (default 16) */
+  int32_t grid_factor;      /* target blocks per SM of the grid, 1..64 (default 16) */
+} sw_scan_shape;
+
+#define SW_SCAN_SIZE_CLASSES 2    /* class 0: lists S of fewer than SW_SCAN_LARGE_ROWS rows; 1: larger */
+#define SW_SCAN_LARGE_ROWS 32768u
+
+int sw_get_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, sw_scan_shape* out);
+/* SW_ERR_INVALID_ARGUMENT for a value outside the lists above, or when two
+ * tiles per warp (8 * words * tile_rows * 2 * warps bytes) exceed 200 KiB. */
+int sw_set_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, const sw_scan_shape* in);
+
+typedef struct {
+  uint32_t words;       /* row width of the key */
+  uint32_t size_class;  /* list size class of the key */
+  uint64_t checks;      /* subset checks of this key in one pass over the automata */
+  double ms_start;      /* their CUDA-event milliseconds (mask build + scan) with the starting shape */
+  double ms_best;       /* with the chosen shape */
+  sw_scan_shape shape;  /* the chosen shape, kept on the context */
+} sw_scan_tuned;
+
+/* Subset-check autotuner: solves the automata one after another on the
+ * context's stream (plan_json; NULL = plain Exact) with every subset check
+ * timed by CUDA events per (words, size class) key, then, knob by knob
+ * (tile_rows 32/64/128, warps 4/8/16, tiles_per_super 4/8/16/32, grid_factor
+ * 4/8/16/32/64), reruns them once per candidate value with that value set for
+ * every key, and each key keeps its fastest value (coordinate descent; a value
+ * must beat the key's best by 2%; best of `reps` passes, 0 = 1).  out (up to
+ * out_cap entries) receives one entry per key the automata used, *out_count
+ * their number.  The chosen shapes stay on the context. */
+int sw_autotune_scan(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                     const char* plan_json, uint32_t reps, sw_scan_tuned* out, uint32_t out_cap,
+                     uint32_t* out_count);
+
 /* ---- measurement --------------------------------------------------------
  * No counterpart in the reference (its timers are host RAII timers,
  * synchrolib/utils/timer.hpp:9-41).  Between sw_profile_begin and

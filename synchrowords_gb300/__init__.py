@@ -114,6 +114,21 @@ class _BatchProfile(ctypes.Structure):
                 ("steps", ctypes.c_uint64), ("graph_replays", ctypes.c_uint32)]
 
 
+class _ScanShape(ctypes.Structure):
+    _fields_ = [("tile_rows", ctypes.c_int32), ("warps", ctypes.c_int32), ("tiles_per_super", ctypes.c_int32),
+                ("grid_factor", ctypes.c_int32)]
+
+
+class _ScanTuned(ctypes.Structure):
+    _fields_ = [("words", ctypes.c_uint32), ("size_class", ctypes.c_uint32), ("checks", ctypes.c_uint64),
+                ("ms_start", ctypes.c_double), ("ms_best", ctypes.c_double), ("shape", _ScanShape)]
+
+
+SCAN_SIZE_CLASSES = 2        # class 0: lists of fewer than SCAN_LARGE_ROWS rows; class 1: larger
+SCAN_LARGE_ROWS = 32768
+DEFAULT_SCAN_SHAPE = {"tile_rows": 64, "warps": 8, "tiles_per_super": 16, "grid_factor": 16}
+
+
 class _KernelProfile(ctypes.Structure):
     _fields_ = [("launches", ctypes.c_uint64), ("ms", ctypes.c_double), ("bytes", ctypes.c_double)]
 
@@ -165,6 +180,10 @@ def load_library():
                                         ctypes.POINTER(_Result), ctypes.POINTER(ctypes.c_int32), ctypes.c_uint32,
                                         ctypes.POINTER(ctypes.c_double), ctypes.c_uint32, ctypes.c_uint32,
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_BatchTuning)]
+    lib.sw_get_scan_shape.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_ScanShape)]
+    lib.sw_set_scan_shape.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_ScanShape)]
+    lib.sw_autotune_scan.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
+                                     ctypes.c_uint32, ctypes.POINTER(_ScanTuned), ctypes.c_uint32, _U32P]
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
                                                      ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32,
                                                      ctypes.c_void_p, ctypes.c_void_p]
@@ -479,6 +498,41 @@ class Context:
                 "cluster_size": int(best.cluster_size), "cluster_limit": float(best.cluster_limit),
                 "ms": {"cluster_size": {int(s): float(t) for s, t in zip(sc, ms[:len(sc)])},
                        "cluster_limit": {float(x): float(t) for x, t in zip(lc, ms[len(sc):])}}}
+
+    def get_scan_shape(self, words: int, size_class: int) -> dict:
+        """Launch shape of the subset check for rows of `words` 64-bit words
+        (1..8) and lists of size class 0 (< SCAN_LARGE_ROWS rows) or 1."""
+        s = _ScanShape()
+        _check(self._lib.sw_get_scan_shape(self._h, words, size_class, ctypes.byref(s)))
+        return {f: int(getattr(s, f)) for f, _ in _ScanShape._fields_}
+
+    def set_scan_shape(self, words: int, size_class: int, tile_rows: int = 64, warps: int = 8,
+                       tiles_per_super: int = 16, grid_factor: int = 16) -> None:
+        """tile_rows 32/64/128, warps 4/8/16, tiles_per_super 4/8/16/32,
+        grid_factor 1..64; results never depend on the shape."""
+        s = _ScanShape(tile_rows, warps, tiles_per_super, grid_factor)
+        _check(self._lib.sw_set_scan_shape(self._h, words, size_class, ctypes.byref(s)))
+
+    def autotune_scan(self, automata: Sequence[Tuple[int, int, Sequence[int]]], plan_json: Optional[str] = None,
+                      reps: int = 1) -> list:
+        """Tune the subset check's launch shape per (words, size class) on the
+        checks these automata's solves make (coordinate descent over tile rows,
+        warps, tiles per super-tile and grid factor, on CUDA-event time); the
+        chosen shapes stay on this context.  One dict per key used: words,
+        size_class, checks, ms_start, ms_best, shape."""
+        if len(automata) == 0:
+            raise ValueError("empty batch")
+        ns, ks, deltas, _, _, _ = self._batch_buffers(automata)
+        out = (_ScanTuned * 16)()
+        cnt = ctypes.c_uint32(0)
+        _check(self._lib.sw_autotune_scan(self._h, len(automata), deltas.ctypes.data_as(_U32P),
+                                          ns.ctypes.data_as(_U32P), ks.ctypes.data_as(_U32P),
+                                          plan_json.encode() if plan_json else None, reps, out, 16,
+                                          ctypes.byref(cnt)))
+        return [{"words": int(o.words), "size_class": int(o.size_class), "checks": int(o.checks),
+                 "ms_start": float(o.ms_start), "ms_best": float(o.ms_best),
+                 "shape": {f: int(getattr(o.shape, f)) for f, _ in _ScanShape._fields_}}
+                for o in out[:min(cnt.value, 16)]]
 
     def get_batch_tuning(self) -> dict:
         t = _BatchTuning()

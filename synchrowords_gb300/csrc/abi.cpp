@@ -561,6 +561,7 @@ int sw_solve_batch(sw_context* ctx, uint32_t count, const uint32_t* deltas, cons
       if (todo.empty()) return;
       const uint32_t nw = std::min<uint32_t>(workers, (uint32_t)todo.size());
       while (ctx->workers.size() + 1 < nw) ctx->workers.push_back(std::make_unique<sw::Solver>(ctx->solver->device()));
+      for (auto& w : ctx->workers) w->set_scan_shapes(ctx->solver->scan_shapes());
       ctx->small.last.streamed += (uint32_t)todo.size();
       std::atomic<size_t> next{0};
       auto work = [&](sw::Solver& solver) {
@@ -803,6 +804,171 @@ int sw_solve_json(sw_context* ctx, const uint32_t* delta, uint32_t n, uint32_t k
   int rc = sw_plan_from_json(plan_json, n, k, &plan);
   if (rc != SW_OK) return rc;
   return sw_solve(ctx, delta, n, k, &plan, r);
+}
+
+namespace {
+constexpr int kKeys = 8 * sw::kScanSizeClasses;  // (words - 1) * size classes + size class
+bool to_shape(const sw_scan_shape& in, sw::ScanShape& out) {
+  out.tile_rows = in.tile_rows;
+  out.warps = in.warps;
+  out.tiles_per_super = in.tiles_per_super;
+  out.grid_factor = in.grid_factor;
+  return true;
+}
+sw_scan_shape from_shape(const sw::ScanShape& s) {
+  sw_scan_shape o;
+  o.tile_rows = s.tile_rows;
+  o.warps = s.warps;
+  o.tiles_per_super = s.tiles_per_super;
+  o.grid_factor = s.grid_factor;
+  return o;
+}
+void set_shapes(sw_context* ctx, const sw::ScanShapes& s) {
+  ctx->solver->set_scan_shapes(s);
+  for (auto& w : ctx->workers) w->set_scan_shapes(s);
+}
+}  // namespace
+
+int sw_get_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, sw_scan_shape* out) {
+  if (!ctx || !out) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (words < 1 || words > 8 || size_class >= SW_SCAN_SIZE_CLASSES)
+    return fail(SW_ERR_INVALID_ARGUMENT, "words must be 1..8 and size_class 0..1");
+  *out = from_shape(ctx->solver->scan_shapes().s[words - 1][size_class]);
+  return SW_OK;
+}
+
+int sw_set_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, const sw_scan_shape* in) {
+  if (!ctx || !in) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (words < 1 || words > 8 || size_class >= SW_SCAN_SIZE_CLASSES)
+    return fail(SW_ERR_INVALID_ARGUMENT, "words must be 1..8 and size_class 0..1");
+  sw::ScanShape sh;
+  to_shape(*in, sh);
+  if (!sw::scan_shape_valid((int)words, sh))
+    return fail(SW_ERR_INVALID_ARGUMENT,
+                "scan shape: tile_rows 32/64/128, warps 4/8/16, tiles_per_super 4/8/16/32, grid_factor 1..64, "
+                "and two tiles per warp within the shared-memory limit");
+  sw::ScanShapes all = ctx->solver->scan_shapes();
+  all.s[words - 1][size_class] = sh;
+  set_shapes(ctx, all);
+  return SW_OK;
+}
+
+int sw_autotune_scan(sw_context* ctx, uint32_t count, const uint32_t* deltas, const uint32_t* ns, const uint32_t* ks,
+                     const char* plan_json, uint32_t reps, sw_scan_tuned* out, uint32_t out_cap,
+                     uint32_t* out_count) {
+  if (!ctx || (count && (!deltas || !ns || !ks)) || (out_cap && !out))
+    return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (count == 0) return fail(SW_ERR_INVALID_ARGUMENT, "empty batch");
+  if (out_count) *out_count = 0;
+  reps = std::max<uint32_t>(reps, 1);
+  const char* json = plan_json ? plan_json : "{\"algorithms\": [{\"name\": \"Exact\"}]}";
+  std::vector<sw_plan> plans(count);
+  std::vector<size_t> off(count + 1, 0);
+  for (uint32_t i = 0; i < count; ++i) {
+    const int rc = sw_plan_from_json(json, ns[i], ks[i], &plans[i]);
+    if (rc != SW_OK) return rc;
+    off[i + 1] = off[i] + (size_t)ns[i] * ks[i];
+  }
+  const sw::ScanShapes start = ctx->solver->scan_shapes();
+  return guarded([&] {
+    // one timed pass: every automaton through the context's solver with the
+    // subset checks timed per key; per key the best of `reps` passes
+    auto pass = [&](double ms[kKeys], uint64_t checks[kKeys]) -> int {
+      for (int i = 0; i < kKeys; ++i) ms[i] = -1;
+      for (uint32_t r = 0; r < reps; ++r) {
+        ctx->solver->profile_begin();
+        for (uint32_t i = 0; i < count; ++i) {
+          sw_result res{};
+          std::string err;
+          const int rc = run_plan(*ctx->solver, deltas + off[i], ns[i], ks[i], &plans[i], &res, err);
+          if (rc != SW_OK) {
+            sw_kernel_profile drop[SW_PROFILE_CLASSES];
+            ctx->solver->profile_end(drop);
+            return fail(rc, err);
+          }
+        }
+        sw_kernel_profile prof[SW_PROFILE_CLASSES];
+        ctx->solver->profile_end(prof);
+        double t[kKeys];
+        ctx->solver->last_scan_profile(t, checks);
+        for (int i = 0; i < kKeys; ++i)
+          if (ms[i] < 0 || t[i] < ms[i]) ms[i] = t[i];
+      }
+      return SW_OK;
+    };
+    double base[kKeys];
+    uint64_t checks[kKeys];
+    int rc = pass(base, checks);
+    if (rc != SW_OK) return rc;
+    double best[kKeys];
+    for (int i = 0; i < kKeys; ++i) best[i] = base[i];
+    sw::ScanShapes top = start;
+    // coordinate descent, every key at once: a knob's candidate value is set
+    // for every key (where the shape stays valid) and each key keeps its
+    // fastest value; a value must beat the key's best by 2% to replace it
+    static const int kTile[3] = {32, 64, 128}, kWarps[3] = {4, 8, 16}, kTps[4] = {4, 8, 16, 32},
+                     kGrid[5] = {4, 8, 16, 32, 64};
+    struct Knob {
+      const int* vals;
+      int n;
+      int sw::ScanShape::*field;
+    };
+    const Knob knobs[4] = {{kTile, 3, &sw::ScanShape::tile_rows},
+                           {kWarps, 3, &sw::ScanShape::warps},
+                           {kTps, 4, &sw::ScanShape::tiles_per_super},
+                           {kGrid, 5, &sw::ScanShape::grid_factor}};
+    for (const Knob& kn : knobs) {
+      const sw::ScanShapes before = top;
+      for (int v = 0; v < kn.n; ++v) {
+        sw::ScanShapes trial = before;
+        bool any = false;
+        for (int key = 0; key < kKeys; ++key) {
+          if (!checks[key]) continue;
+          sw::ScanShape sh = before.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses];
+          if (sh.*kn.field == kn.vals[v]) continue;  // already timed
+          sh.*kn.field = kn.vals[v];
+          if (!sw::scan_shape_valid(key / sw::kScanSizeClasses + 1, sh)) continue;
+          trial.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses] = sh;
+          any = true;
+        }
+        if (!any) continue;
+        set_shapes(ctx, trial);
+        double t[kKeys];
+        uint64_t c2[kKeys];
+        rc = pass(t, c2);
+        if (rc != SW_OK) {
+          set_shapes(ctx, start);
+          return rc;
+        }
+        for (int key = 0; key < kKeys; ++key) {
+          const int w = key / sw::kScanSizeClasses, c = key % sw::kScanSizeClasses;
+          if (!checks[key] || !(trial.s[w][c].*kn.field == kn.vals[v]) || before.s[w][c].*kn.field == kn.vals[v])
+            continue;
+          if (t[key] < 0.98 * best[key]) {
+            best[key] = t[key];
+            top.s[w][c] = trial.s[w][c];
+          }
+        }
+      }
+    }
+    set_shapes(ctx, top);
+    uint32_t n_out = 0;
+    for (int key = 0; key < kKeys; ++key) {
+      if (!checks[key]) continue;
+      if (n_out < out_cap) {
+        sw_scan_tuned& o = out[n_out];
+        o.words = (uint32_t)(key / sw::kScanSizeClasses + 1);
+        o.size_class = (uint32_t)(key % sw::kScanSizeClasses);
+        o.checks = checks[key];
+        o.ms_start = base[key];
+        o.ms_best = best[key];
+        o.shape = from_shape(top.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses]);
+      }
+      ++n_out;
+    }
+    if (out_count) *out_count = n_out;
+    return SW_OK;
+  });
 }
 
 int sw_profile_begin(sw_context* ctx) {

@@ -141,6 +141,7 @@ class Engine {
     if (!d_query_bytes) SW_CUDA(cudaMalloc(&d_query_bytes, sizeof(u64)));
     SW_CUDA(cudaMemsetAsync(d_query_bytes, 0, sizeof(u64), stream));
     for (auto& c : prof) c = ProfClass{};
+    scan_ev.clear();
     ev_next = 0;
     prof_on = true;
   }
@@ -159,6 +160,16 @@ class Engine {
       out[c].launches = prof[c].launches;
       out[c].ms = ms;
       out[c].bytes = prof[c].bytes;
+    }
+    for (int i = 0; i < 8 * kScanSizeClasses; ++i) {
+      scan_ms[i] = 0;
+      scan_launches[i] = 0;
+    }
+    for (auto& kv : scan_ev) {
+      float t = 0;
+      SW_CUDA(cudaEventElapsedTime(&t, kv.second.first, kv.second.second));
+      scan_ms[kv.first] += t;
+      scan_launches[kv.first]++;
     }
     prof_on = false;
   }
@@ -249,18 +260,36 @@ class Engine {
     count_launch(launches);
   }
 
-  // Subset queries run on the tiled check (subset_check.cu).
+  // Subset queries run on the tiled check (subset_check.cu), in the launch
+  // shape the context holds for the row width and the list's size class.
   DevBuf tile_and;
+  ScanShapes scan_shapes;
+  // while profiling: events around each check's mask build + scan, keyed by
+  // (W - 1) * kScanSizeClasses + size class
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> scan_ev;
+  double scan_ms[8 * kScanSizeClasses] = {};
+  u64 scan_launches[8 * kScanSizeClasses] = {};
 
   void query(int W, int mode, const u64* S, u32 m, const u64* Q, u32 q, int n, u32* flags, bool stop) {
     if (!m || !q) return;
-    tile_and.reserve(subset_check_temp_bytes(W, m));
-    timed(3, (double)m * 8.0 * W, [&] { launch_tile_and(W, S, m, tile_and.as<u64>(), stream); });
+    const ScanShape& sh = scan_shapes.pick(W, m);
+    tile_and.reserve(subset_check_temp_bytes(W, m, sh));
+    cudaEvent_t e0 = nullptr;
+    if (prof_on) {
+      e0 = next_event();
+      SW_CUDA(cudaEventRecord(e0, stream));
+    }
+    timed(3, (double)m * 8.0 * W, [&] { launch_tile_and(W, S, m, tile_and.as<u64>(), sh, stream); });
     // algorithmic bytes: the query rows plus every S tile staged on chip
     timed(0, (double)q * 8.0 * W, [&] {
-      launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, stream,
+      launch_subset_check(W, mode, S, m, tile_and.as<u64>(), Q, q, n, flags, d_misc, stop, sh, stream,
                           prof_on ? d_query_bytes : nullptr, d_misc + kScanErrWord);
     });
+    if (prof_on) {
+      cudaEvent_t e1 = next_event();
+      SW_CUDA(cudaEventRecord(e1, stream));
+      scan_ev.push_back({(W - 1) * kScanSizeClasses + (m >= kScanLargeRows ? 1 : 0), {e0, e1}});
+    }
     count_launch(2);
     if (st) {
       st->trie_queries += q;
@@ -644,6 +673,14 @@ void Solver::profile_begin() {
 void Solver::profile_end(sw_kernel_profile out[4]) {
   SW_CUDA(cudaSetDevice(device_));
   eng_->profile_end(out);
+}
+void Solver::set_scan_shapes(const ScanShapes& s) { eng_->scan_shapes = s; }
+const ScanShapes& Solver::scan_shapes() const { return eng_->scan_shapes; }
+void Solver::last_scan_profile(double ms[8 * kScanSizeClasses], uint64_t checks[8 * kScanSizeClasses]) const {
+  for (int i = 0; i < 8 * kScanSizeClasses; ++i) {
+    ms[i] = eng_->scan_ms[i];
+    checks[i] = eng_->scan_launches[i];
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -9,6 +9,7 @@
 #include "../../include/synchrowords.h"
 #include "automaton.hpp"
 #include "common.cuh"
+#include "kernels.cuh"
 
 namespace sw {
 
@@ -84,6 +85,12 @@ class Solver {
   // Per-kernel-class CUDA-event timing of everything launched in between.
   void profile_begin();
   void profile_end(sw_kernel_profile out[4]);
+  // Launch shapes of the subset check per row width and list size class.
+  void set_scan_shapes(const ScanShapes& s);
+  const ScanShapes& scan_shapes() const;
+  // CUDA-event milliseconds and count of the subset checks (mask build plus
+  // scan) of the last profiled interval, per (W - 1) * kScanSizeClasses + size class.
+  void last_scan_profile(double ms[8 * kScanSizeClasses], uint64_t checks[8 * kScanSizeClasses]) const;
 
  private:
   int device_;

@@ -72,16 +72,39 @@ enum QueryMode : int {
 // Tiled subset check (subset_check.cu): for each query row c, flags[c] |=
 // hit(c) (or, with `stop`, record one witness pair and let all warps exit
 // early: witness[0] = found flag, witness[1] = query index, witness[2] = set
-// index).  S is cut into 64-row tiles; tile_and[t] (W words) = AND of the
-// tile's rows, from launch_tile_and.  `flags` must start zeroed (non-stop
+// index).  S is cut into tiles of sh.tile_rows rows; tile_and[t] (W words) =
+// AND of the tile's rows, then one mask per super-tile of
+// sh.tiles_per_super tiles, from launch_tile_and with the same shape.  `flags` must start zeroed (non-stop
 // mode).  `bytes_ctr` (optional) accumulates the bytes of S tiles staged on
 // chip.  S must start 16-byte aligned (its tiles move by bulk copies).  *err
 // is set to 1 when a wait for a tile copy runs out (its bounded poll limit);
 // the results of that launch are then incomplete.
-size_t subset_check_temp_bytes(int W, u32 m);
-void launch_tile_and(int W, const u64* S, u32 m, u64* tile_and, cudaStream_t s);
+// Launch shape of the subset check: rows of S per staged tile (32, 64, 128),
+// warps of 32 queries per block (4, 8, 16), tiles per super-tile mask (4, 8,
+// 16, 32) and the grid's target blocks per SM (1..64), which sets how finely
+// S is chunked over blockIdx.y.  Results do not depend on it.
+struct ScanShape {
+  int tile_rows = 64;
+  int warps = 8;
+  int tiles_per_super = 16;
+  int grid_factor = 16;
+};
+// Shapes per row width W (1..8) and list size class: class 0 for lists S of
+// fewer than kScanLargeRows rows, class 1 for larger ones.
+constexpr int kScanSizeClasses = 2;
+constexpr u32 kScanLargeRows = 1u << 15;
+constexpr size_t kMaxScanSmem = 200 * 1024;
+struct ScanShapes {
+  ScanShape s[8][kScanSizeClasses];
+  const ScanShape& pick(int W, u32 m) const { return s[W - 1][m >= kScanLargeRows ? 1 : 0]; }
+};
+bool scan_shape_valid(int W, const ScanShape& sh);
+size_t scan_smem_bytes(int W, const ScanShape& sh);
+size_t subset_check_temp_bytes(int W, u32 m, const ScanShape& sh);
+void launch_tile_and(int W, const u64* S, u32 m, u64* tile_and, const ScanShape& sh, cudaStream_t s);
 void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* tile_and, const u64* Q, u32 q, int n,
-                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr, u32* err);
+                         u32* flags, u32* witness, bool stop, const ScanShape& sh, cudaStream_t s, u64* bytes_ctr,
+                         u32* err);
 
 // out = sorted merge of two sorted, mutually disjoint row arrays.
 void launch_merge(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* out, cudaStream_t s);

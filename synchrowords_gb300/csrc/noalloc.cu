@@ -30,8 +30,9 @@ namespace sw {
 namespace {
 
 // masks for SW_NOALLOC_MAX_SETS rows of 8 words: one per 64-row tile plus one
-// per 1024-row super-tile (see subset_check.cu), plus 4 words: three for the
-// unused meet-mode witness, one for the kernel's copy-timeout word
+// per 1024-row super-tile (the default ScanShape, which this entry point
+// always uses, whatever shapes a context was tuned to), plus 4 words: three
+// for the unused meet-mode witness, one for the kernel's copy-timeout word
 constexpr size_t kMaxTiles = (SW_NOALLOC_MAX_SETS + 63) / 64;
 constexpr size_t kMaxSupers = (SW_NOALLOC_MAX_SETS + 1023) / 1024;
 constexpr size_t kScratchWords = (kMaxTiles + kMaxSupers) * 8 + 4;  // + witness, error word
@@ -128,10 +129,12 @@ extern "C" int sw_subsets_check_device_noalloc(uint32_t n, const uint64_t* d_set
   auto* masks = static_cast<u64*>(scratch);
   u32* witness = reinterpret_cast<u32*>(masks + kScratchWords - 4);
   try {
-    launch_tile_and(W, reinterpret_cast<const u64*>(d_sets), (u32)set_count, masks, s);
+    const ScanShape sh{};
+    static_assert(ScanShape{}.tile_rows == 64 && ScanShape{}.tiles_per_super == 16, "scratch sized for 64 x 16");
+    launch_tile_and(W, reinterpret_cast<const u64*>(d_sets), (u32)set_count, masks, sh, s);
     launch_subset_check(W, proper ? kQueryProperSubset : kQuerySubset, reinterpret_cast<const u64*>(d_sets),
                         (u32)set_count, masks, reinterpret_cast<const u64*>(d_checks), (u32)check_count, (int)n,
-                        d_results, witness, false, s, nullptr, witness + 3);
+                        d_results, witness, false, sh, s, nullptr, witness + 3);
   } catch (const std::exception& ex) {
     g_err = ex.what();
     return SW_ERR_CUDA;

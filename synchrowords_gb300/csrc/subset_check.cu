@@ -6,7 +6,10 @@
 // kernel cuda/subsets_implicit_trie_kernel.cu:13-92).  The trie's pruning is
 // re-expressed as a prefix-partitioned candidate filter:
 //   * S is sorted (lexicographically, most frequent states first) and cut into
-//     tiles of 64 consecutive rows, grouped 16 to a super-tile;
+//     tiles of 64 consecutive rows, grouped 16 to a super-tile (the default
+//     ScanShape; tile rows, tiles per super-tile, warps per block and the
+//     grid's S chunking are runtime parameters that the kernel autotuner
+//     picks per row width and list size);
 //   * every tile and super-tile keeps the AND of its rows — the states all of
 //     its sets contain.  For sorted rows that is the range's common prefix
 //     (the trie node's path) plus incidental shared states;
@@ -29,36 +32,58 @@
 namespace sw {
 
 namespace {
-constexpr int kTileRows = 64;
-constexpr int kTilesPerSuper = 16;
-constexpr int kSuperRows = kTileRows * kTilesPerSuper;
-constexpr int kWarps = 8;
+constexpr int kMaxScanWarps = 16;
+constexpr int kMaxTilesPerSuper = 32;
 constexpr u32 kMinChunkTiles = 4;
 constexpr u32 kFullMask = 0xffffffffu;
 
 int sm_count_sc() { return device_sm_count(); }
 
-__host__ __device__ inline u32 n_tiles(u32 m) { return (m + kTileRows - 1) / kTileRows; }
-__host__ __device__ inline u32 n_supers(u32 m) { return (m + kSuperRows - 1) / kSuperRows; }
+int log2_exact(int v) {
+  int l = 0;
+  while ((1 << l) < v) ++l;
+  return l;
+}
+u32 n_tiles(u32 m, const ScanShape& sh) { return (m + sh.tile_rows - 1) / (u32)sh.tile_rows; }
+u32 n_supers(u32 m, const ScanShape& sh) {
+  const u32 rows = (u32)sh.tile_rows * (u32)sh.tiles_per_super;
+  return (m + rows - 1) / rows;
+}
 }  // namespace
 
-// AND masks: tiles first (n_tiles(m) entries), then super-tiles.  One block
-// per super-tile, one warp per tile: each lane ANDs two rows, a butterfly
-// combines the lanes, and warp 0 folds the block's tile masks into the
-// super-tile's mask (so no mask needs presetting and no atomics are used).
+bool scan_shape_valid(int W, const ScanShape& sh) {
+  const bool pow2_tr = sh.tile_rows == 32 || sh.tile_rows == 64 || sh.tile_rows == 128;
+  const bool warps = sh.warps == 4 || sh.warps == 8 || sh.warps == 16;
+  const bool tps = sh.tiles_per_super == 4 || sh.tiles_per_super == 8 || sh.tiles_per_super == 16 ||
+                   sh.tiles_per_super == 32;
+  const bool grid = sh.grid_factor >= 1 && sh.grid_factor <= 64;
+  return W >= 1 && W <= 8 && pow2_tr && warps && tps && grid && scan_smem_bytes(W, sh) <= kMaxScanSmem;
+}
+
+size_t scan_smem_bytes(int W, const ScanShape& sh) {
+  return sizeof(u64) * (size_t)W * (size_t)sh.tile_rows * 2 * (size_t)sh.warps;  // two tiles per warp
+}
+
+// AND masks: tiles first (n_tiles entries), then super-tiles.  One block per
+// super-tile, one warp per tile: each lane ANDs the tile's rows lane,
+// lane + 32, ..., a butterfly combines the lanes, and warp 0 folds the
+// block's tile masks into the super-tile's mask (so no mask needs presetting
+// and no atomics are used).
 template <int W>
-__global__ void __launch_bounds__(kTilesPerSuper * 32) k_range_and(const u64* __restrict__ S, u32 m,
-                                                                   u64* __restrict__ masks) {
-  __shared__ u64 s_and[kTilesPerSuper][W];
-  const u32 tiles = n_tiles(m);
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const u32 t = blockIdx.x * kTilesPerSuper + warp;
+__global__ void __launch_bounds__(kMaxTilesPerSuper * 32) k_range_and(const u64* __restrict__ S, u32 m,
+                                                                      u64* __restrict__ masks, int tile_rows) {
+  __shared__ u64 s_and[kMaxTilesPerSuper][W];
+  const u32 tiles = (m + tile_rows - 1) / (u32)tile_rows;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, tps = blockDim.x >> 5;
+  const u32 t = blockIdx.x * tps + warp;
   u64* super_and = masks + (size_t)tiles * W;
-  const u32 r0 = t * kTileRows + lane, r1 = r0 + 32;
 #pragma unroll
   for (int w = 0; w < W; ++w) {
-    u64 a = r0 < m ? S[(size_t)r0 * W + w] : ~0ULL;
-    if (r1 < m) a &= S[(size_t)r1 * W + w];
+    u64 a = ~0ULL;
+    for (int i = lane; i < tile_rows; i += 32) {
+      const u32 r = t * (u32)tile_rows + (u32)i;
+      if (r < m) a &= S[(size_t)r * W + w];
+    }
 #pragma unroll
     for (int o = 16; o; o >>= 1) a &= __shfl_xor_sync(kFullMask, a, o);
     if (lane == 0) {
@@ -69,8 +94,7 @@ __global__ void __launch_bounds__(kTilesPerSuper * 32) k_range_and(const u64* __
   __syncthreads();
   if (warp == 0 && lane < W) {
     u64 a = ~0ULL;
-#pragma unroll
-    for (int x = 0; x < kTilesPerSuper; ++x) a &= s_and[x][lane];
+    for (int x = 0; x < tps; ++x) a &= s_and[x][lane];
     super_and[(size_t)blockIdx.x * W + lane] = a;
   }
 }
@@ -106,17 +130,25 @@ __device__ __forceinline__ bool mbar_wait(u64* bar, u32 parity) {
   return false;
 }
 
-template <int W, int MODE>
-__global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restrict__ S, u32 m,
-                                                             const u64* __restrict__ masks, u32 tiles_per_chunk,
-                                                             const u64* __restrict__ Q, u32 q, int n,
-                                                             u32* __restrict__ flags, u32* witness, int stop,
-                                                             u64* __restrict__ bytes_ctr, u32* err) {
-  // per warp: two tile buffers of 64 rows, filled by bulk copies
-  extern __shared__ __align__(128) u64 s_tiles[];  // [kWarps][2][kTileRows * W]
-  __shared__ __align__(8) u64 s_bar[kWarps][2];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const u32 qi = (blockIdx.x * kWarps + warp) * 32 + lane;
+// Tile rows TR are a template parameter (a runtime row count costs ten
+// registers); tiles per super-tile (1 << tps_log2) and the block's warps
+// (blockDim.x / 32) are runtime parameters.
+template <int W, int MODE, int TR>
+__global__ void __launch_bounds__(kMaxScanWarps * 32) k_subset_scan(const u64* __restrict__ S, u32 m,
+                                                                    const u64* __restrict__ masks,
+                                                                    u32 tiles_per_chunk, const u64* __restrict__ Q,
+                                                                    u32 q, int n, u32* __restrict__ flags,
+                                                                    u32* witness, int stop,
+                                                                    u64* __restrict__ bytes_ctr, u32* err,
+                                                                    int tps_log2) {
+  // per warp: two tile buffers of tile_rows rows, filled by bulk copies
+  extern __shared__ __align__(128) u64 s_tiles[];  // [warps][2][tile_rows * W]
+  __shared__ __align__(8) u64 s_bar[kMaxScanWarps][2];
+  constexpr u32 kTileRows = TR;
+  constexpr int tr_log2 = TR == 32 ? 5 : TR == 64 ? 6 : 7;
+  static_assert(TR == 32 || TR == 64 || TR == 128, "tile rows");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  const u32 qi = (blockIdx.x * warps + warp) * 32 + lane;
   const bool valid = qi < q;
   u64 c[W];
 #pragma unroll
@@ -128,7 +160,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
   bool hit = false;
   u32 hit_idx = 0;
   u64 loaded = 0;
-  const u32 tiles = n_tiles(m);
+  const u32 tiles = (m + kTileRows - 1) >> tr_log2;
   const u64* tile_and = masks;
   const u64* super_and = masks + (size_t)tiles * W;
   // buffer b of this warp; bit b of par = phase parity its next copy completes
@@ -149,14 +181,14 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
   auto advance = [&](u32 from) -> u32 {
     bool need_s = false;
     for (u32 t = from; t < t1; ++t) {
-      if (t == from || t % kTilesPerSuper == 0) {
-        const u32 sp = t / kTilesPerSuper;
+      if (t == from || (t & ((1u << tps_log2) - 1)) == 0) {
+        const u32 sp = t >> tps_log2;
         need_s = !done;
 #pragma unroll
         for (int w = 0; w < W; ++w)
           if (super_and[(size_t)sp * W + w] & ~c[w]) need_s = false;
         if (!__any_sync(kFullMask, need_s)) {
-          t = min(t1, (sp + 1) * kTilesPerSuper) - 1;  // skip the rest of this super-tile
+          t = min(t1, (sp + 1) << tps_log2) - 1;  // skip the rest of this super-tile
           continue;
         }
       }
@@ -169,12 +201,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
     return t1;
   };
   // full tiles move as one bulk copy; the last, partial tile of S with plain loads
-  auto full_tile = [&](u32 t) { return (t + 1) * (u32)kTileRows <= m; };
+  auto full_tile = [&](u32 t) { return (t + 1) * kTileRows <= m; };
   auto issue = [&](u32 t, int b) {
     if (!full_tile(t)) return;
     if (lane == 0) {
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier reads of the buffer come first
-      bulk_load(buf(b), S + (size_t)t * kTileRows * W, (u32)(kTileRows * W * 8), bar0 + b);
+      bulk_load(buf(b), S + (size_t)t * kTileRows * W, kTileRows * W * 8, bar0 + b);
     }
   };
   bool failed = false;
@@ -188,7 +220,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
       u64* const d = buf(b);
       for (u32 i = lane; i < rows * W; i += 32) d[i] = S[(size_t)r0 * W + i];
       // rows past the end of S never pass the word-0 test below
-      for (u32 i = rows * W + lane; i < (u32)kTileRows * W; i += 32) d[i] = ~0ULL;
+      for (u32 i = rows * W + lane; i < kTileRows * W; i += 32) d[i] = ~0ULL;
       __syncwarp();
     }
   };
@@ -205,7 +237,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
       if (nxt < t1 && full_tile(nxt)) mbar_wait(bar0 + (b ^ 1), (par >> (b ^ 1)) & 1u);  // bounded
       return;
     }
-    const u32 rows = min((u32)kTileRows, m - cur * kTileRows);
+    const u32 rows = min(kTileRows, m - cur * kTileRows);
     loaded += rows;
     bool need = !done;
 #pragma unroll
@@ -216,7 +248,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
       const u64 nc0 = ~c[0];
       // four rows per iteration: independent word-0 tests, full test only
       // for the (rare) rows that pass
-      for (u32 r = 0; r < (u32)kTileRows && !done; r += 4) {
+      for (u32 r = 0; r < kTileRows && !done; r += 4) {
         const u64 a0 = my_rows[(r + 0) * W], a1 = my_rows[(r + 1) * W];
         const u64 a2 = my_rows[(r + 2) * W], a3 = my_rows[(r + 3) * W];
         const unsigned pass = (!(a0 & nc0) ? 1u : 0u) | (!(a1 & nc0) ? 2u : 0u) | (!(a2 & nc0) ? 4u : 0u) |
@@ -251,7 +283,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
     }
     // leave when every lane is decided or, in meet mode, once any warp met
     bool leave = __all_sync(kFullMask, done);
-    const u32 sp = nxt / kTilesPerSuper;
+    const u32 sp = nxt >> tps_log2;
     if (!leave && stop && nxt < t1 && sp != last_super) {
       last_super = sp;
       u32 f = lane == 0 ? *(volatile u32*)witness : 0u;
@@ -270,56 +302,73 @@ __global__ void __launch_bounds__(kWarps * 32) k_subset_scan(const u64* __restri
   if (hit && !stop) flags[qi] = 1u;
 }
 
-size_t subset_check_temp_bytes(int W, u32 m) {
-  return sizeof(u64) * (size_t)W * (n_tiles(std::max<u32>(m, 1)) + n_supers(std::max<u32>(m, 1)) + 1);
+size_t subset_check_temp_bytes(int W, u32 m, const ScanShape& sh) {
+  const u32 mm = std::max<u32>(m, 1);
+  return sizeof(u64) * (size_t)W * (n_tiles(mm, sh) + n_supers(mm, sh) + 1);
 }
 
-void launch_tile_and(int W, const u64* S, u32 m, u64* masks, cudaStream_t s) {
+void launch_tile_and(int W, const u64* S, u32 m, u64* masks, const ScanShape& sh, cudaStream_t s) {
   if (!m) return;
-  const u32 blocks = n_supers(m);
+  if (!scan_shape_valid(W, sh)) throw std::invalid_argument("range_and: invalid scan shape");
+  const u32 blocks = n_supers(m, sh);
+  const int threads = sh.tiles_per_super * 32;
+#define SW_RA(WW) \
+  case WW: k_range_and<WW><<<blocks, threads, 0, s>>>(S, m, masks, sh.tile_rows); break;
   switch (W) {
-    case 1: k_range_and<1><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 2: k_range_and<2><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 3: k_range_and<3><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 4: k_range_and<4><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 5: k_range_and<5><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 6: k_range_and<6><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 7: k_range_and<7><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
-    case 8: k_range_and<8><<<blocks, kTilesPerSuper * 32, 0, s>>>(S, m, masks); break;
+    SW_RA(1)
+    SW_RA(2)
+    SW_RA(3)
+    SW_RA(4)
+    SW_RA(5)
+    SW_RA(6)
+    SW_RA(7)
+    SW_RA(8)
     default: throw std::runtime_error("range_and: unsupported width");
   }
+#undef SW_RA
   SW_LAUNCH_CHECK();
 }
 
 void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks, const u64* Q, u32 q, int n,
-                         u32* flags, u32* witness, bool stop, cudaStream_t s, u64* bytes_ctr, u32* err) {
+                         u32* flags, u32* witness, bool stop, const ScanShape& sh, cudaStream_t s, u64* bytes_ctr,
+                         u32* err) {
   if (!m || !q) return;
   if (!err) throw std::invalid_argument("subset check: an error word is required");
-  const u32 tiles = n_tiles(m);
-  const u32 qblocks = (q + kWarps * 32 - 1) / (kWarps * 32);
-  // split S into chunks of tiles so that the grid covers the GPU ~16x: per-warp
-  // work varies a lot (early exits, filter hit rates), and many small blocks
-  // keep the SMs busy until the slowest ones finish.  A chunk keeps at least
-  // kMinChunkTiles tiles so that loading the warp's queries stays amortised.
-  const u32 target = (u32)sm_count_sc() * 16;
+  if (!scan_shape_valid(W, sh)) throw std::invalid_argument("subset check: invalid scan shape");
+  const u32 tiles = n_tiles(m, sh);
+  const u32 qrows = (u32)sh.warps * 32;
+  const u32 qblocks = (q + qrows - 1) / qrows;
+  // split S into chunks of tiles so that the grid covers the GPU grid_factor
+  // times: per-warp work varies a lot (early exits, filter hit rates), and
+  // many small blocks keep the SMs busy until the slowest ones finish.  A
+  // chunk keeps at least kMinChunkTiles tiles so that loading the warp's
+  // queries stays amortised.
+  const u32 target = (u32)sm_count_sc() * (u32)sh.grid_factor;
   u32 chunks = std::max<u32>(1, (target + qblocks - 1) / qblocks);
   chunks = std::min<u32>(chunks, std::max<u32>(1, tiles / kMinChunkTiles));
   chunks = std::min<u32>(chunks, 65535);
   const u32 per = (tiles + chunks - 1) / chunks;
   chunks = (tiles + per - 1) / per;
   dim3 grid(qblocks, chunks);
-  const size_t smem = sizeof(u64) * (size_t)W * kTileRows * 2 * kWarps;  // two tiles per warp
-#define SW_SC_ONE(WW, MM)                                                                                     \
-  {                                                                                                           \
-    if (smem >= 32 * 1024) ensure_smem_limit((const void*)k_subset_scan<WW, MM>, (int)smem);               \
-    k_subset_scan<WW, MM><<<grid, kWarps * 32, smem, s>>>(S, m, masks, per, Q, q, n, flags, witness, stop, \
-                                                          bytes_ctr, err);                                   \
+  const size_t smem = scan_smem_bytes(W, sh);
+  const int tps_log2 = log2_exact(sh.tiles_per_super);
+#define SW_SC_TR(WW, MM, TT)                                                                                      \
+  {                                                                                                               \
+    if (smem >= 32 * 1024) ensure_smem_limit((const void*)k_subset_scan<WW, MM, TT>, (int)smem);               \
+    k_subset_scan<WW, MM, TT><<<grid, qrows, smem, s>>>(S, m, masks, per, Q, q, n, flags, witness, stop, bytes_ctr, \
+                                                        err, tps_log2);                                          \
   }
-#define SW_SC(WW)                                                   \
-  case WW:                                                          \
-    if (mode == kQuerySubset) SW_SC_ONE(WW, kQuerySubset)           \
+#define SW_SC_ONE(WW, MM)                                 \
+  {                                                       \
+    if (sh.tile_rows == 32) SW_SC_TR(WW, MM, 32)          \
+    else if (sh.tile_rows == 64) SW_SC_TR(WW, MM, 64)     \
+    else SW_SC_TR(WW, MM, 128)                            \
+  }
+#define SW_SC(WW)                                                          \
+  case WW:                                                                 \
+    if (mode == kQuerySubset) SW_SC_ONE(WW, kQuerySubset)                  \
     else if (mode == kQueryProperSubset) SW_SC_ONE(WW, kQueryProperSubset) \
-    else SW_SC_ONE(WW, kQueryDisjoint)                              \
+    else SW_SC_ONE(WW, kQueryDisjoint)                                     \
     break;
   switch (W) {
     SW_SC(1)
@@ -335,6 +384,7 @@ void launch_subset_check(int W, int mode, const u64* S, u32 m, const u64* masks,
   }
 #undef SW_SC
 #undef SW_SC_ONE
+#undef SW_SC_TR
   SW_LAUNCH_CHECK();
 }
 

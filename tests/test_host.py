@@ -57,6 +57,9 @@ def test_batch_entry_points_reject_null_arguments(native_lib):
     assert lib.sw_autotune_batch(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
     assert lib.sw_autotune_cluster(None, 1, None, None, None, b"{}", None, None, 0, None, 0, 1, None, None) == -1
     assert lib.sw_batch_last_profile(None, None) == -1
+    assert lib.sw_get_scan_shape(None, 4, 0, None) == -1
+    assert lib.sw_set_scan_shape(None, 4, 0, None) == -1
+    assert lib.sw_autotune_scan(None, 1, None, None, None, None, 1, None, 0, None) == -1
     assert lib.sw_mlp_train_ranked(None, None, 0, None, None, None, None, None, None, None, 0.0, 1, 1, 0.0, 0,
                                    None) == -1
     assert b"NULL" in lib.sw_last_error()
