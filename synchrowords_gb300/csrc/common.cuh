@@ -62,6 +62,23 @@ int device_sm_count();
 // another host thread never sees its limit lowered below what it asked for.
 void ensure_smem_limit(const void* fn, int bytes);
 
+// Stream on which the calling thread's DevBuf growth is ordered (set by an
+// AllocScope around a search on one stream).  With one, growing a buffer
+// frees the old block and takes the new one stream-ordered
+// (cudaFreeAsync / cudaMallocAsync from the device's default pool, which the
+// scope keeps cached), so the grow waits for nothing but that stream;
+// without one it uses cudaFree, which waits for every stream of the device.
+// Buffers grown inside a scope must only be used on that stream, or after it
+// has been synchronised.
+cudaStream_t& alloc_stream();
+struct AllocScope {
+  cudaStream_t prev;
+  explicit AllocScope(cudaStream_t s);
+  ~AllocScope() { alloc_stream() = prev; }
+  AllocScope(const AllocScope&) = delete;
+  AllocScope& operator=(const AllocScope&) = delete;
+};
+
 // Grow-only device buffer (the context keeps them across steps and solves,
 // so a solve performs no per-step cudaMalloc).
 struct DevBuf {
@@ -75,10 +92,18 @@ struct DevBuf {
   }
   void reserve(size_t bytes) {
     if (bytes <= cap) return;
-    if (p) SW_CUDA(cudaFree(p));
-    p = nullptr;
-    size_t want = bytes + bytes / 4 + 256;
-    SW_CUDA(cudaMalloc(&p, want));
+    const size_t want = bytes + bytes / 4 + 256;
+    if (cudaStream_t s = alloc_stream()) {
+      if (p) SW_CUDA(cudaFreeAsync(p, s));
+      p = nullptr;
+      cap = 0;
+      SW_CUDA(cudaMallocAsync(&p, want, s));
+    } else {
+      if (p) SW_CUDA(cudaFree(p));
+      p = nullptr;
+      cap = 0;
+      SW_CUDA(cudaMalloc(&p, want));
+    }
     cap = want;
   }
   void release() {

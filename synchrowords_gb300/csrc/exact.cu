@@ -50,13 +50,21 @@ struct Side {
   double unique_growth = 0;      // distinct children per parent at the last step
   KeyMap keymap;                 // sort key of this side's layers and visited list
   bool keymap_chosen = false;
-  // Layers of earlier solves, kept with their device buffers: freeing device
-  // memory synchronises the whole device, which would stall every other
-  // solve running on the GPU at the time.
+  // Layers of earlier solves, kept with their device buffers, so that a
+  // solve's layers reuse them instead of allocating: a new layer takes the
+  // spare whose origin buffer holds `origin_bytes` with the least room to
+  // spare, else the largest (which then grows).
   std::vector<std::unique_ptr<Layer>> spare;
-  std::unique_ptr<Layer> new_layer() {
+  std::unique_ptr<Layer> new_layer(size_t origin_bytes) {
     if (spare.empty()) return std::make_unique<Layer>();
-    std::unique_ptr<Layer> L = std::move(spare.back());
+    size_t best = 0;
+    for (size_t i = 1; i < spare.size(); ++i) {
+      const size_t c = spare[i]->origin.cap, cb = spare[best]->origin.cap;
+      const bool fits = c >= origin_bytes, best_fits = cb >= origin_bytes;
+      if (fits ? (!best_fits || c < cb) : (!best_fits && c > cb)) best = i;
+    }
+    std::unique_ptr<Layer> L = std::move(spare[best]);
+    spare[best] = std::move(spare.back());
     spare.pop_back();
     L->count = L->parent_count = 0;
     return L;
@@ -173,12 +181,41 @@ class Engine {
     }
     prof_on = false;
   }
-  u32* d_misc = nullptr;  // [0..3] witness, [8] scan total, [kScanErrWord] subset-scan copy timeout
+  u32* d_misc = nullptr;  // [0..3] witness, [8] scan total, [kScanErrWord] bounded-wait timeouts
   static constexpr int kScanErrWord = 4;  // read back with the witness, never cleared by it
-  // Throws if a subset-check launch reported a tile copy that never arrived
-  // (its bounded wait ran out); `w` is the pinned copy of d_misc[kScanErrWord].
+  // Throws if a launch reported a bounded wait that ran out: 1 = a subset
+  // check's tile copy never arrived, 2 = a compaction tile's look-back never
+  // saw its predecessor; `w` is the pinned copy of d_misc[kScanErrWord].
   static void check_scan_error(u32 w) {
+    if (w == 2) throw CudaError("layer compaction: a look-back wait ran out");
     if (w) throw CudaError("subset check: a tile copy did not complete within its wait limit");
+  }
+  // Single-pass duplicate removal (launch_dedup_compact): its tile status
+  // words (zero-filled when allocated), tile counter and launch epoch.
+  DevBuf dc_status, dc_ctr;
+  size_t dc_status_zeroed = 0;
+  u32 dc_epoch = 0;
+  u32 next_dc_epoch(u32 m) {
+    const size_t words = dedup_compact_status_words(m);
+    if (!dc_ctr.p) {
+      dc_ctr.reserve(sizeof(u32));
+      SW_CUDA(cudaMemsetAsync(dc_ctr.p, 0, sizeof(u32), stream));
+    }
+    if (++dc_epoch >= (1u << 30)) dc_epoch = 0;  // wrapped: every word back to "unpublished"
+    if (dc_status.cap < sizeof(u64) * words || dc_epoch == 0) {
+      dc_status.reserve(sizeof(u64) * std::max<size_t>(words, (size_t)1 << 16));
+      SW_CUDA(cudaMemsetAsync(dc_status.p, 0, dc_status.cap, stream));
+      if (dc_epoch == 0) dc_epoch = 1;
+    }
+    return dc_epoch;
+  }
+  // The compaction's count and the timeout word in one read-back.
+  u32 read_total_checked() {
+    SW_CUDA(cudaMemcpyAsync(pinned.p, d_misc + kScanErrWord, 5 * sizeof(u32), cudaMemcpyDeviceToHost, stream));
+    SW_CUDA(cudaStreamSynchronize(stream));
+    const u32* w = pinned.as<u32>();
+    check_scan_error(w[0]);
+    return w[8 - kScanErrWord];
   }
   // tables
   DevBuf t_delta, t_beg, t_src;
@@ -349,27 +386,22 @@ class Engine {
     sort_rows(2, keys.as<u64>(), ch_vals.as<u32>(), Nc);
     if (dominance && !self_check && !visited_subsets) {
       // duplicates only: a child is dropped when it equals its predecessor in
-      // the sorted layer or a visited set — one flag pass over the children in
-      // sort order (rows read through the sort's permutation), one compaction
-      // that gathers the kept rows and writes their origins into the new layer
-      timed(3, (double)Nc * 8.0 * W, [&] {
-        launch_dedup_flags(W, ch_rows.as<u64>(), ch_vals.as<u32>(), keys.as<u64>(), Nc, X.vis.as<u64>(),
-                           X.vis_count, X.keymap, flags_a.as<u32>(), stream);
+      // the sorted layer or a visited set.  One launch flags the children in
+      // sort order (rows read through the sort's permutation), counts the
+      // kept ones before each tile by decoupled look-back, and gathers the
+      // kept rows and their origins into the new layer.
+      X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(Nc, 1));
+      std::unique_ptr<Layer> L = X.new_layer(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
+      L->origin.reserve(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
+      u32* total = d_misc + 8;
+      const u32 epoch = next_dc_epoch(Nc);
+      timed(3, (double)Nc * (4 + 16 + 8.0 * W) + (double)Nc * (8.0 * W + 4), [&] {
+        launch_dedup_compact(W, ch_rows.as<u64>(), ch_vals.as<u32>(), keys.as<u64>(), Nc, X.vis.as<u64>(),
+                             X.vis_count, X.keymap, X.rows_alt.as<u64>(), L->origin.as<u32>(), total,
+                             dc_status.as<u64>(), dc_ctr.as<u32>(), epoch, d_misc + kScanErrWord, stream);
       });
       count_launch();
-      X.rows_alt.reserve(sizeof(u64) * W * (size_t)std::max<u32>(Nc, 1));
-      std::unique_ptr<Layer> L = X.new_layer();
-      L->origin.reserve(sizeof(u32) * (size_t)std::max<u32>(Nc, 1));
-      pos.reserve(sizeof(u32) * (size_t)Nc);
-      scan_tmp.reserve(scan_temp_bytes(Nc));
-      u32* total = d_misc + 8;
-      timed(3, (double)Nc * (4 + 4 + 4 + 8.0 * W + 4), [&] {
-        launch_scan(flags_a.as<u32>(), pos.as<u32>(), Nc, total, scan_tmp.p, stream);
-        launch_compact_gather(W, ch_rows.as<u64>(), ch_vals.as<u32>(), flags_a.as<u32>(), pos.as<u32>(), Nc,
-                              X.rows_alt.as<u64>(), L->origin.as<u32>(), stream);
-      });
-      count_launch(2);
-      const u32 f = read_u32(total);
+      const u32 f = read_total_checked();
       if (m) X.unique_growth = (double)f / m;
       if (verbose)
         std::fprintf(stderr, "[sw] %s parents=%u children=%u kept=%u (duplicates only) | %.3f ms\n",
@@ -393,7 +425,7 @@ class Engine {
         st->subsets_kept += u;
         st->dfs_sets += u;
       }
-      auto L = X.new_layer();
+      auto L = X.new_layer(sizeof(u32) * std::max<u32>(u, 1));
       L->origin.reserve(sizeof(u32) * std::max<u32>(u, 1));
       if (u) SW_CUDA(cudaMemcpyAsync(L->origin.p, uq_vals.p, sizeof(u32) * u, cudaMemcpyDeviceToDevice, stream));
       L->count = u;
@@ -458,7 +490,7 @@ class Engine {
     X.count = f;
     if (st) st->subsets_kept += f;
     if (!L) {
-      L = X.new_layer();
+      L = X.new_layer(sizeof(u32) * std::max<u32>(f, 1));
       L->origin.reserve(sizeof(u32) * std::max<u32>(f, 1));
       if (f)
         SW_CUDA(cudaMemcpyAsync(L->origin.p, new_vals.p, sizeof(u32) * f, cudaMemcpyDeviceToDevice, stream));
@@ -731,6 +763,7 @@ void Solver::exact(const Automaton& A0, const sw_exact_config& cfg, Bounds& b, s
   }
   SW_CUDA(cudaSetDevice(device_));
   Engine& E = *eng_;
+  AllocScope alloc_scope(E.stream);  // buffer growth ordered on this solve's stream only
   E.st = &st;
   auto t0 = std::chrono::steady_clock::now();
   const int n = (int)A.n, k = (int)A.k, W = words_for(n);
@@ -1031,7 +1064,7 @@ static BeamRun beam_cutoff(Engine& E, const Automaton& A, u32 beam_size, u64 max
     E.count_launch();
     std::swap(X.rows.p, X.rows_alt.p);
     std::swap(X.rows.cap, X.rows_alt.cap);
-    auto L = X.new_layer();
+    auto L = X.new_layer(sizeof(u32) * std::max<u32>(keep, 1));
     L->origin.reserve(sizeof(u32) * std::max<u32>(keep, 1));
     SW_CUDA(cudaMemcpyAsync(L->origin.p, E.uq_vals.p, sizeof(u32) * keep, cudaMemcpyDeviceToDevice, E.stream));
     L->count = keep;
@@ -1052,6 +1085,7 @@ void Solver::beam(const Automaton& A0, const sw_beam_config& cfg, Bounds& b, sw_
   }
   SW_CUDA(cudaSetDevice(device_));
   Engine& E = *eng_;
+  AllocScope alloc_scope(E.stream);  // buffer growth ordered on this solve's stream only
   E.st = &st;
   auto t0 = std::chrono::steady_clock::now();
   // presort (beam.hpp:54-63, 351-369): states ordered by in-degree ascending

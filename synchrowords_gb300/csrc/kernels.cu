@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <set>
 #include <utility>
 #include <vector>
 
@@ -32,6 +33,30 @@ int device_sm_count() {
   std::lock_guard<std::mutex> g(g_devinfo_mu);
   if (!cached[dev]) SW_CUDA(cudaDeviceGetAttribute(&cached[dev], cudaDevAttrMultiProcessorCount, dev));
   return cached[dev];
+}
+
+cudaStream_t& alloc_stream() {
+  thread_local cudaStream_t s = nullptr;
+  return s;
+}
+
+AllocScope::AllocScope(cudaStream_t s) : prev(alloc_stream()) {
+  // keep freed blocks in the device's default pool instead of returning them
+  // to the driver at every synchronisation (this process's pool only)
+  static std::mutex mu;
+  static std::set<int> cached;
+  int dev = 0;
+  SW_CUDA(cudaGetDevice(&dev));
+  {
+    std::lock_guard<std::mutex> g(mu);
+    if (cached.insert(dev).second) {
+      cudaMemPool_t pool;
+      SW_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+      uint64_t keep = ~0ull;
+      SW_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+  }
+  alloc_stream() = s;
 }
 
 void ensure_smem_limit(const void* fn, int bytes) {
@@ -976,15 +1001,14 @@ void launch_clear_members(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32
   SW_LAUNCH_CHECK();
 }
 
-// Fused duplicate removal over a key-sorted layer, without materialising the
-// sorted rows: position i of the sort holds child vals[i] of C (its layer key
-// keys[2i..2i+1]); flags[i] = 1 when that child differs from child vals[i-1]
+// Duplicate test over a key-sorted layer, without materialising the sorted
+// rows: position i of the sort holds child vals[i] of C (its layer key
+// keys[2i..2i+1]); it is kept when that child differs from child vals[i-1]
 // and equals no row of the key-sorted visited list V.
 template <int W>
-__global__ void k_dedup_flags(const u64* __restrict__ C, const u32* __restrict__ vals, const u64* __restrict__ keys,
-                              u32 m, const u64* __restrict__ V, u32 nv, KeyMap map, u32* __restrict__ flags) {
-  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+__device__ __forceinline__ bool dedup_keep(const u64* __restrict__ C, const u32* __restrict__ vals,
+                                           const u64* __restrict__ keys, u32 i, const u64* __restrict__ V, u32 nv,
+                                           const KeyMap& map) {
   const u64* x = C + (size_t)vals[i] * W;
   bool keep = i == 0 || !row_eq<W>(x, C + (size_t)vals[i - 1] * W);
   if (keep && nv) {
@@ -1005,33 +1029,113 @@ __global__ void k_dedup_flags(const u64* __restrict__ C, const u32* __restrict__
       if (row_eq<W>(x, y)) keep = false;
     }
   }
-  flags[i] = keep ? 1u : 0u;
+  return keep;
 }
 
-// out_rows[pos[i]] = C[vals[i]], out_vals[pos[i]] = vals[i] for the flagged i.
+// ---- single-pass duplicate removal and compaction ----
+// One launch flags the children, counts the kept ones and gathers them: each
+// block takes the next tile of kDcTile children (a dynamic tile index from
+// `ctr`, so every tile a block waits on belongs to a block that is already
+// running), flags its children, scans the flags in shared memory, and finds
+// the count kept before its tile by decoupled look-back over the earlier
+// tiles' published words: (flag << 62) | (epoch << 32) | count, flag 1 = the
+// tile's own count, 2 = the inclusive count of every tile up to it.  `epoch`
+// (1..2^30-1, new per launch) tags the words, so the array is never cleared.
+// Every wait polls at most kDcWaitLimit times; one that runs out sets *err
+// to 2 and the launch's output is incomplete.  The block that drew the last
+// tile index resets `ctr` for the next launch on the stream and stores the
+// total.
+constexpr u32 kDcTile = 512;
+constexpr u32 kDcWaitLimit = 1u << 22;
+
+__device__ __forceinline__ u64 ld_acquire_u64(const u64* p) {
+  u64 v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(u64* p, u64 v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 template <int W>
-__global__ void k_compact_gather(const u64* __restrict__ C, const u32* __restrict__ vals,
-                                 const u32* __restrict__ flags, const u32* __restrict__ pos, u32 m,
-                                 u64* __restrict__ out_rows, u32* __restrict__ out_vals) {
-  const u32 i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m || !flags[i]) return;
-  const u32 d = pos[i], src = vals[i];
+__global__ void __launch_bounds__(kDcTile) k_dedup_compact(const u64* __restrict__ C, const u32* __restrict__ vals,
+                                                          const u64* __restrict__ keys, u32 m,
+                                                          const u64* __restrict__ V, u32 nv, KeyMap map,
+                                                          u64* __restrict__ out_rows, u32* __restrict__ out_vals,
+                                                          u32* total, u64* status, u32* ctr, u32 epoch, u32* err) {
+  __shared__ u32 s_tile, s_warp[kDcTile / 32], s_excl;
+  const u32 ntiles = (m + kDcTile - 1) / kDcTile;
+  if (threadIdx.x == 0) s_tile = atomicAdd(ctr, 1u);
+  __syncthreads();
+  const u32 tile = s_tile;
+  if (threadIdx.x == 0 && tile == ntiles - 1) *ctr = 0u;  // every block has drawn its index
+  const u32 i = tile * kDcTile + threadIdx.x;
+  const bool keep = i < m && dedup_keep<W>(C, vals, keys, i, V, nv, map);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const u32 ballot = __ballot_sync(0xffffffffu, keep);
+  const u32 before_in_warp = __popc(ballot & ((1u << lane) - 1u));
+  if (lane == 0) s_warp[warp] = __popc(ballot);
+  __syncthreads();
+  if (warp == 0) {
+    const u32 c = lane < kDcTile / 32 ? s_warp[lane] : 0u;
+    u32 incl = c;
 #pragma unroll
-  for (int w = 0; w < W; ++w) out_rows[(size_t)d * W + w] = C[(size_t)src * W + w];
-  out_vals[d] = src;
+    for (int o = 1; o < 32; o <<= 1) {
+      const u32 y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const u32 agg = __shfl_sync(0xffffffffu, incl, 31);
+    if (lane < kDcTile / 32) s_warp[lane] = incl - c;  // exclusive count of the earlier warps
+    if (lane == 0) {
+      const u64 tag = (u64)(epoch & 0x3fffffffu) << 32;
+      u32 excl = 0;
+      if (tile == 0) {
+        st_release_u64(status, (2ull << 62) | tag | agg);
+      } else {
+        st_release_u64(status + tile, (1ull << 62) | tag | agg);
+        u32 j = tile - 1, polls = 0;
+        for (;;) {
+          const u64 w = ld_acquire_u64(status + j);
+          const u32 f = (u32)(w >> 62);
+          if (f == 0 || (w & (0x3fffffffull << 32)) != tag) {  // not published yet
+            if (++polls > kDcWaitLimit) {
+              atomicExch(err, 2u);
+              break;
+            }
+            continue;
+          }
+          excl += (u32)w;
+          if (f == 2 || j == 0) break;
+          --j;
+        }
+        st_release_u64(status + tile, (2ull << 62) | tag | (excl + agg));
+      }
+      s_excl = excl;
+      if (tile == ntiles - 1) *total = excl + agg;
+    }
+  }
+  __syncthreads();
+  if (keep) {
+    const u32 d = s_excl + s_warp[warp] + before_in_warp, src = vals[i];
+#pragma unroll
+    for (int w = 0; w < W; ++w) out_rows[(size_t)d * W + w] = C[(size_t)src * W + w];
+    out_vals[d] = src;
+  }
 }
 
-void launch_dedup_flags(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
-                        const KeyMap& map, u32* flags, cudaStream_t s) {
-  if (!m) return;
-  SW_DISPATCH_W(W, (k_dedup_flags<WW><<<(m + 255) / 256, 256, 0, s>>>(C, vals, keys, m, V, nv, map, flags)));
-  SW_LAUNCH_CHECK();
-}
+size_t dedup_compact_status_words(u32 m) { return (m + kDcTile - 1) / kDcTile; }
 
-void launch_compact_gather(int W, const u64* C, const u32* vals, const u32* flags, const u32* pos, u32 m,
-                           u64* out_rows, u32* out_vals, cudaStream_t s) {
-  if (!m) return;
-  SW_DISPATCH_W(W, (k_compact_gather<WW><<<(m + 255) / 256, 256, 0, s>>>(C, vals, flags, pos, m, out_rows, out_vals)));
+void launch_dedup_compact(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
+                          const KeyMap& map, u64* out_rows, u32* out_vals, u32* total, u64* status, u32* ctr,
+                          u32 epoch, u32* err, cudaStream_t s) {
+  if (!m) {
+    SW_CUDA(cudaMemsetAsync(total, 0, sizeof(u32), s));
+    return;
+  }
+  if (epoch == 0 || epoch >= (1u << 30)) throw std::invalid_argument("dedup_compact: epoch must be 1..2^30-1");
+  const u32 blocks = (m + kDcTile - 1) / kDcTile;
+  SW_DISPATCH_W(W, (k_dedup_compact<WW><<<blocks, kDcTile, 0, s>>>(C, vals, keys, m, V, nv, map, out_rows, out_vals,
+                                                                  total, status, ctr, epoch, err)));
   SW_LAUNCH_CHECK();
 }
 

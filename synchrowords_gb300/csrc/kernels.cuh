@@ -127,14 +127,20 @@ void launch_merge_key(int W, const u64* A, u32 na, const u64* B, u32 nb, u64* ou
                       const KeyMap& map = KeyMap{});
 // flags[i] = 1 if row i of C equals a row of V (flags untouched otherwise);
 // V and C sorted by the same layer key.
-// Duplicate removal of a key-sorted layer in one pass: flags[i] = 1 when
-// child vals[i] of C differs from child vals[i-1] and equals no row of the
-// key-sorted visited list V (keys = the children's sorted layer keys).
-void launch_dedup_flags(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
-                        const KeyMap& map, u32* flags, cudaStream_t s);
-// out_rows[pos[i]] = C[vals[i]], out_vals[pos[i]] = vals[i] for the flagged i.
-void launch_compact_gather(int W, const u64* C, const u32* vals, const u32* flags, const u32* pos, u32 m,
-                           u64* out_rows, u32* out_vals, cudaStream_t s);
+// Duplicate removal of a key-sorted layer and compaction in one launch
+// (decoupled look-back over tiles): child vals[i] of C is kept when it
+// differs from child vals[i-1] and equals no row of the key-sorted visited
+// list V (keys = the children's sorted layer keys); out_rows / out_vals
+// receive the kept children in sort order, *total their count.  `status`
+// holds dedup_compact_status_words(m) words (zero-filled when first
+// allocated), `ctr` one word that is zero before the first launch (each
+// launch leaves it zero); `epoch` is 1..2^30-1 and must differ from the
+// previous launch's on the same status array.  *err is set to 2 if a bounded
+// wait ran out.
+size_t dedup_compact_status_words(u32 m);
+void launch_dedup_compact(int W, const u64* C, const u32* vals, const u64* keys, u32 m, const u64* V, u32 nv,
+                          const KeyMap& map, u64* out_rows, u32* out_vals, u32* total, u64* status, u32* ctr,
+                          u32 epoch, u32* err, cudaStream_t s);
 void launch_member_key(int W, const u64* V, u32 nv, const u64* C, u32 nc, u32* flags, cudaStream_t s,
                        const KeyMap& map = KeyMap{});
 // flags[i] = 0 where flags[i] = 1 and row i of C equals a row of V (same

@@ -19,8 +19,10 @@
 // super-tiles of its chunk of S: a range is skipped unless some lane still
 // needs it (__any_sync).  Needed tiles move into the warp's two shared-memory
 // buffers by 1-D bulk copies (cp.async.bulk, completion on one mbarrier per
-// buffer): while the lanes test their queries against one tile, with an
-// early exit on word 0, the next needed tile is already on its way.  No block-wide
+// buffer): while the warp tests one tile — lanes holding the tile's rows,
+// the needing queries broadcast one at a time, ballots over the rows' first
+// words, the full test only for rows that pass — the next needed tile is
+// already on its way.  No block-wide
 // barriers: warps of a block proceed independently.  Warps stop as soon as all
 // their queries are decided; in meet mode the first hit stops the grid.
 #include <cuda_runtime.h>
@@ -244,32 +246,62 @@ __global__ void __launch_bounds__(kMaxScanWarps * 32) k_subset_scan(const u64* _
     for (int w = 0; w < W; ++w)
       if (tile_and[(size_t)cur * W + w] & ~c[w]) need = false;
     const u64* my_rows = buf(b);
-    if (need) {
-      const u64 nc0 = ~c[0];
-      // four rows per iteration: independent word-0 tests, full test only
-      // for the (rare) rows that pass
-      for (u32 r = 0; r < kTileRows && !done; r += 4) {
-        const u64 a0 = my_rows[(r + 0) * W], a1 = my_rows[(r + 1) * W];
-        const u64 a2 = my_rows[(r + 2) * W], a3 = my_rows[(r + 3) * W];
-        const unsigned pass = (!(a0 & nc0) ? 1u : 0u) | (!(a1 & nc0) ? 2u : 0u) | (!(a2 & nc0) ? 4u : 0u) |
-                              (!(a3 & nc0) ? 8u : 0u);
-        if (!pass) continue;
+    // Warp-cooperative test: the lanes hold the tile's rows (lane l rows l,
+    // l + 32, ...) and the warp walks only the queries that still need this
+    // tile, one at a time: the query's first word is broadcast, every lane
+    // tests its rows' first words against it, and ballots collect the rows
+    // that pass; only those rows get the full test (their other words
+    // against the broadcast query), and the first row that holds gives the
+    // hit.  A tile costs a few instructions per needing query instead of a
+    // pass over all its rows whenever any lane needs it.
+    u32 needy = __ballot_sync(kFullMask, need);
+    if (needy) {
+      constexpr int kRowsPerLane = TR / 32;
+      u64 r0[kRowsPerLane];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          if (!((pass >> j) & 1u) || r + j >= rows) continue;
-          const u64* s = my_rows + (r + j) * W;
-          bool sub = true, eq = (s[0] == c[0]);
+      for (int t = 0; t < kRowsPerLane; ++t) {
+        const u32 r = (u32)t * 32 + lane;
+        // rows past the end of S take no part (a query may hold every state of word 0)
+        r0[t] = r < rows ? my_rows[(size_t)r * W] : ~0ULL;
+      }
+      while (needy) {
+        const int j = __ffs(needy) - 1;
+        needy &= needy - 1;
+        const u64 nc0 = ~__shfl_sync(kFullMask, c[0], j);
+        u32 pass[kRowsPerLane];
+        u32 any_pass = 0;
+#pragma unroll
+        for (int t = 0; t < kRowsPerLane; ++t) {
+          pass[t] = __ballot_sync(kFullMask, !(r0[t] & nc0) && (u32)t * 32 + lane < rows);
+          any_pass |= pass[t];
+        }
+        if (!any_pass) continue;
+        int hit_row = -1;
+        for (int t = 0; t < kRowsPerLane; ++t) {
+          if (!pass[t]) continue;  // warp-uniform
+          bool sub = (pass[t] >> lane) & 1u;
+          bool eq = sub && r0[t] == ~nc0;
+          const u64* srow = my_rows + (size_t)((u32)t * 32 + lane) * W;
 #pragma unroll
           for (int w = 1; w < W; ++w) {
-            sub = sub && !(s[w] & ~c[w]);
-            eq = eq && (s[w] == c[w]);
+            const u64 cw = __shfl_sync(kFullMask, c[w], j);  // every lane takes part in the broadcast
+            if (sub) {
+              const u64 sw = srow[w];
+              sub = !(sw & ~cw);
+              eq = eq && (sw == cw);
+            }
           }
-          if (sub && (MODE != kQueryProperSubset || !eq)) {
-            hit = true;
-            done = true;
-            hit_idx = cur * kTileRows + r + j;
+          if (MODE == kQueryProperSubset && eq) sub = false;
+          const u32 hits = __ballot_sync(kFullMask, sub);
+          if (hits) {
+            hit_row = t * 32 + __ffs(hits) - 1;
             break;
           }
+        }
+        if (hit_row >= 0 && lane == j) {
+          hit = true;
+          done = true;
+          hit_idx = cur * kTileRows + (u32)hit_row;
         }
       }
     }
