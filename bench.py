@@ -283,6 +283,8 @@ def run_ours(args, world, rank, local):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
     tuned = tuned_c = tuned_scan = None
+    if args.scan_tune < 0:  # default: tune where a held-out pass takes seconds, not minutes
+        args.scan_tune = 8 if n <= 256 else (2 if n <= 320 else 0)
     if args.scan_tune:
         # untimed: the subset check's launch shape tuned on held-out automata of the same shape
         tuned_scan = ctx.autotune_scan(workload_dfas(args.workload, rank, args.scan_tune), plan)
@@ -416,9 +418,10 @@ def main():
     ap.add_argument("--streams", type=int, default=16, help="concurrent device streams (host threads)")
     ap.add_argument("--autotune", action="store_true",
                     help="before the warm-up, tune the batch's worker count and batched-launch limit on the workload")
-    ap.add_argument("--scan-tune", type=int, default=0, metavar="N",
+    ap.add_argument("--scan-tune", type=int, default=-1, metavar="N",
                     help="before the warm-up, tune the subset check's launch shape on N held-out automata of the "
-                         "workload's shape (0 = the default shape)")
+                         "workload's shape (0 = the default shape; default: 8 up to n = 256, 2 at n = 320, "
+                         "0 above)")
     ap.add_argument("--learned-vs-plain", type=int, default=0, metavar="N",
                     help="also solve the first N n=384 automata plainly (12 GB and GPU-sized budgets) and with the "
                          "learned bound, and report their wall times (minutes per automaton; off by default)")
