@@ -870,104 +870,121 @@ int sw_autotune_scan(sw_context* ctx, uint32_t count, const uint32_t* deltas, co
     off[i + 1] = off[i] + (size_t)ns[i] * ks[i];
   }
   const sw::ScanShapes start = ctx->solver->scan_shapes();
+  bool profiling = false;
+  // a failed tuning leaves the context as it found it: its starting shapes,
+  // profiling off
+  auto restore = [&] {
+    set_shapes(ctx, start);
+    if (profiling) {
+      profiling = false;
+      try {
+        sw_kernel_profile drop[SW_PROFILE_CLASSES];
+        ctx->solver->profile_end(drop);
+      } catch (...) {
+      }
+    }
+  };
   return guarded([&] {
-    // one timed pass: every automaton through the context's solver with the
-    // subset checks timed per key; per key the best of `reps` passes
-    auto pass = [&](double ms[kKeys], uint64_t checks[kKeys]) -> int {
-      for (int i = 0; i < kKeys; ++i) ms[i] = -1;
-      for (uint32_t r = 0; r < reps; ++r) {
-        ctx->solver->profile_begin();
-        for (uint32_t i = 0; i < count; ++i) {
-          sw_result res{};
-          std::string err;
-          const int rc = run_plan(*ctx->solver, deltas + off[i], ns[i], ks[i], &plans[i], &res, err);
-          if (rc != SW_OK) {
-            sw_kernel_profile drop[SW_PROFILE_CLASSES];
-            ctx->solver->profile_end(drop);
-            return fail(rc, err);
+    try {
+      // one timed pass: every automaton through the context's solver with the
+      // subset checks timed per key; per key the best of `reps` passes
+      auto pass = [&](double ms[kKeys], uint64_t checks[kKeys]) -> int {
+        for (int i = 0; i < kKeys; ++i) ms[i] = -1;
+        for (uint32_t r = 0; r < reps; ++r) {
+          ctx->solver->profile_begin();
+          profiling = true;
+          for (uint32_t i = 0; i < count; ++i) {
+            sw_result res{};
+            std::string err;
+            const int rc = run_plan(*ctx->solver, deltas + off[i], ns[i], ks[i], &plans[i], &res, err);
+            if (rc != SW_OK) {
+              restore();
+              return fail(rc, err);
+            }
+          }
+          sw_kernel_profile prof[SW_PROFILE_CLASSES];
+          profiling = false;
+          ctx->solver->profile_end(prof);
+          double t[kKeys];
+          ctx->solver->last_scan_profile(t, checks);
+          for (int i = 0; i < kKeys; ++i)
+            if (ms[i] < 0 || t[i] < ms[i]) ms[i] = t[i];
+        }
+        return SW_OK;
+      };
+      double base[kKeys];
+      uint64_t checks[kKeys];
+      int rc = pass(base, checks);
+      if (rc != SW_OK) return rc;
+      double best[kKeys];
+      for (int i = 0; i < kKeys; ++i) best[i] = base[i];
+      sw::ScanShapes top = start;
+      // coordinate descent, every key at once: a knob's candidate value is set
+      // for every key (where the shape stays valid) and each key keeps its
+      // fastest value; a value must beat the key's best by 2% to replace it
+      static const int kTile[3] = {32, 64, 128}, kWarps[3] = {4, 8, 16}, kTps[4] = {4, 8, 16, 32},
+                       kGrid[5] = {4, 8, 16, 32, 64};
+      struct Knob {
+        const int* vals;
+        int n;
+        int sw::ScanShape::*field;
+      };
+      const Knob knobs[4] = {{kTile, 3, &sw::ScanShape::tile_rows},
+                             {kWarps, 3, &sw::ScanShape::warps},
+                             {kTps, 4, &sw::ScanShape::tiles_per_super},
+                             {kGrid, 5, &sw::ScanShape::grid_factor}};
+      for (const Knob& kn : knobs) {
+        const sw::ScanShapes before = top;
+        for (int v = 0; v < kn.n; ++v) {
+          sw::ScanShapes trial = before;
+          bool any = false;
+          for (int key = 0; key < kKeys; ++key) {
+            if (!checks[key]) continue;
+            sw::ScanShape sh = before.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses];
+            if (sh.*kn.field == kn.vals[v]) continue;  // already timed
+            sh.*kn.field = kn.vals[v];
+            if (!sw::scan_shape_valid(key / sw::kScanSizeClasses + 1, sh)) continue;
+            trial.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses] = sh;
+            any = true;
+          }
+          if (!any) continue;
+          set_shapes(ctx, trial);
+          double t[kKeys];
+          uint64_t c2[kKeys];
+          rc = pass(t, c2);
+          if (rc != SW_OK) return rc;  // pass() restored the context
+          for (int key = 0; key < kKeys; ++key) {
+            const int w = key / sw::kScanSizeClasses, c = key % sw::kScanSizeClasses;
+            if (!checks[key] || !(trial.s[w][c].*kn.field == kn.vals[v]) || before.s[w][c].*kn.field == kn.vals[v])
+              continue;
+            if (t[key] < 0.98 * best[key]) {
+              best[key] = t[key];
+              top.s[w][c] = trial.s[w][c];
+            }
           }
         }
-        sw_kernel_profile prof[SW_PROFILE_CLASSES];
-        ctx->solver->profile_end(prof);
-        double t[kKeys];
-        ctx->solver->last_scan_profile(t, checks);
-        for (int i = 0; i < kKeys; ++i)
-          if (ms[i] < 0 || t[i] < ms[i]) ms[i] = t[i];
       }
+      set_shapes(ctx, top);
+      uint32_t n_out = 0;
+      for (int key = 0; key < kKeys; ++key) {
+        if (!checks[key]) continue;
+        if (n_out < out_cap) {
+          sw_scan_tuned& o = out[n_out];
+          o.words = (uint32_t)(key / sw::kScanSizeClasses + 1);
+          o.size_class = (uint32_t)(key % sw::kScanSizeClasses);
+          o.checks = checks[key];
+          o.ms_start = base[key];
+          o.ms_best = best[key];
+          o.shape = from_shape(top.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses]);
+        }
+        ++n_out;
+      }
+      if (out_count) *out_count = n_out;
       return SW_OK;
-    };
-    double base[kKeys];
-    uint64_t checks[kKeys];
-    int rc = pass(base, checks);
-    if (rc != SW_OK) return rc;
-    double best[kKeys];
-    for (int i = 0; i < kKeys; ++i) best[i] = base[i];
-    sw::ScanShapes top = start;
-    // coordinate descent, every key at once: a knob's candidate value is set
-    // for every key (where the shape stays valid) and each key keeps its
-    // fastest value; a value must beat the key's best by 2% to replace it
-    static const int kTile[3] = {32, 64, 128}, kWarps[3] = {4, 8, 16}, kTps[4] = {4, 8, 16, 32},
-                     kGrid[5] = {4, 8, 16, 32, 64};
-    struct Knob {
-      const int* vals;
-      int n;
-      int sw::ScanShape::*field;
-    };
-    const Knob knobs[4] = {{kTile, 3, &sw::ScanShape::tile_rows},
-                           {kWarps, 3, &sw::ScanShape::warps},
-                           {kTps, 4, &sw::ScanShape::tiles_per_super},
-                           {kGrid, 5, &sw::ScanShape::grid_factor}};
-    for (const Knob& kn : knobs) {
-      const sw::ScanShapes before = top;
-      for (int v = 0; v < kn.n; ++v) {
-        sw::ScanShapes trial = before;
-        bool any = false;
-        for (int key = 0; key < kKeys; ++key) {
-          if (!checks[key]) continue;
-          sw::ScanShape sh = before.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses];
-          if (sh.*kn.field == kn.vals[v]) continue;  // already timed
-          sh.*kn.field = kn.vals[v];
-          if (!sw::scan_shape_valid(key / sw::kScanSizeClasses + 1, sh)) continue;
-          trial.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses] = sh;
-          any = true;
-        }
-        if (!any) continue;
-        set_shapes(ctx, trial);
-        double t[kKeys];
-        uint64_t c2[kKeys];
-        rc = pass(t, c2);
-        if (rc != SW_OK) {
-          set_shapes(ctx, start);
-          return rc;
-        }
-        for (int key = 0; key < kKeys; ++key) {
-          const int w = key / sw::kScanSizeClasses, c = key % sw::kScanSizeClasses;
-          if (!checks[key] || !(trial.s[w][c].*kn.field == kn.vals[v]) || before.s[w][c].*kn.field == kn.vals[v])
-            continue;
-          if (t[key] < 0.98 * best[key]) {
-            best[key] = t[key];
-            top.s[w][c] = trial.s[w][c];
-          }
-        }
-      }
+    } catch (...) {
+      restore();
+      throw;
     }
-    set_shapes(ctx, top);
-    uint32_t n_out = 0;
-    for (int key = 0; key < kKeys; ++key) {
-      if (!checks[key]) continue;
-      if (n_out < out_cap) {
-        sw_scan_tuned& o = out[n_out];
-        o.words = (uint32_t)(key / sw::kScanSizeClasses + 1);
-        o.size_class = (uint32_t)(key % sw::kScanSizeClasses);
-        o.checks = checks[key];
-        o.ms_start = base[key];
-        o.ms_best = best[key];
-        o.shape = from_shape(top.s[key / sw::kScanSizeClasses][key % sw::kScanSizeClasses]);
-      }
-      ++n_out;
-    }
-    if (out_count) *out_count = n_out;
-    return SW_OK;
   });
 }
 
