@@ -366,3 +366,22 @@ def test_multi_rank_max_and_disjoint_shards():
         p.join(timeout=60)
     assert [v for _, v, _ in out] == [20.0, 20.0]  # max over ranks
     assert out[0][2] != out[1][2]  # each rank solves its own automata (weak scaling)
+
+
+def test_bench_scan_tuning_uses_held_out_automata():
+    """The bench tunes the subset check's launch shape on automata of the
+    workload's shape that no rank's timed workload contains."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    for name in ("n200", "n48", "n320", "batch4096"):
+        for rank in (0, 1):
+            timed = {tuple(d) for _, _, d in bench.workload_dfas(name, rank)}
+            held = bench.workload_dfas(name, rank, held_out=4)
+            assert len(held) == 4
+            n, k, _, _, _ = bench.WORKLOADS[name]
+            if n:
+                assert all((a[0], a[1]) == (n, k) for a in held)
+            for other in (0, 1):
+                timed_other = {tuple(d) for _, _, d in bench.workload_dfas(name, other)}
+                assert not any(tuple(d) in timed_other for _, _, d in held), (name, rank, other)
+            assert not any(tuple(d) in timed for _, _, d in held)
