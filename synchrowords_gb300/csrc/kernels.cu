@@ -583,7 +583,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_bitonic_small(u64* keys, u32*
           sp[hi] = pa;
         }
       }
-      __syncthreads();
+      // Thread t handles pair t (N / 2 <= kSmallThreads).  At a distance
+      // j <= 32 every pair of warp w lies in rows [64w, 64w + 64), so
+      // between two such stages only the warp's own lanes exchange rows and
+      // a warp barrier suffices; any stage at a larger distance, and the
+      // read-out after the last stage, needs the block barrier.
+      const u32 next_j = j > 1 ? j >> 1 : kk;
+      if (j <= 32 && next_j <= 32 && !(kk == N && j == 1)) __syncwarp();
+      else __syncthreads();
     }
   }
   for (u32 i = threadIdx.x; i < m; i += kSmallThreads) {
