@@ -308,6 +308,10 @@ typedef struct {
 #define SW_SCAN_LARGE_ROWS 32768u
 
 int sw_get_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, sw_scan_shape* out);
+/* SW_OK when `shape` is a valid launch shape for rows of `words` words (the
+ * rule sw_set_scan_shape applies), else SW_ERR_INVALID_ARGUMENT with the
+ * reason in sw_last_error().  Host-only: needs no device. */
+int sw_scan_shape_check(uint32_t words, const sw_scan_shape* shape);
 /* SW_ERR_INVALID_ARGUMENT for a value outside the lists above, or when two
  * tiles per warp (8 * words * tile_rows * 2 * warps bytes) exceed 200 KiB. */
 int sw_set_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, const sw_scan_shape* in);

@@ -182,6 +182,7 @@ def load_library():
                                         ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_BatchTuning)]
     lib.sw_get_scan_shape.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_ScanShape)]
     lib.sw_set_scan_shape.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_ScanShape)]
+    lib.sw_scan_shape_check.argtypes = [ctypes.c_uint32, ctypes.POINTER(_ScanShape)]
     lib.sw_autotune_scan.argtypes = [ctypes.c_void_p, ctypes.c_uint32, _U32P, _U32P, _U32P, ctypes.c_char_p,
                                      ctypes.c_uint32, ctypes.POINTER(_ScanTuned), ctypes.c_uint32, _U32P]
     lib.sw_subsets_check_device_noalloc.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint64,
@@ -225,6 +226,14 @@ def eval_expression(expr: str, n: int, k: int) -> Tuple[int, float]:
     d = ctypes.c_double()
     _check(load_library().sw_eval_expression(expr.encode(), n, k, ctypes.byref(u), ctypes.byref(d)))
     return u.value, d.value
+
+
+def check_scan_shape(words: int, tile_rows: int = 64, warps: int = 8, tiles_per_super: int = 16,
+                     grid_factor: int = 16) -> None:
+    """Raise SynchroError unless this is a valid subset-check launch shape for
+    rows of `words` 64-bit words (host-only; needs no device)."""
+    s = _ScanShape(tile_rows, warps, tiles_per_super, grid_factor)
+    _check(load_library().sw_scan_shape_check(words, ctypes.byref(s)))
 
 
 def plan_from_json(text: str, n: int, k: int) -> dict:

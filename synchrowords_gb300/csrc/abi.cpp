@@ -837,16 +837,27 @@ int sw_get_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, sw_s
   return SW_OK;
 }
 
-int sw_set_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, const sw_scan_shape* in) {
-  if (!ctx || !in) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
-  if (words < 1 || words > 8 || size_class >= SW_SCAN_SIZE_CLASSES)
-    return fail(SW_ERR_INVALID_ARGUMENT, "words must be 1..8 and size_class 0..1");
+int sw_scan_shape_check(uint32_t words, const sw_scan_shape* shape) {
+  if (!shape) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (words < 1 || words > 8) return fail(SW_ERR_INVALID_ARGUMENT, "words must be 1..8");
   sw::ScanShape sh;
-  to_shape(*in, sh);
+  to_shape(*shape, sh);
   if (!sw::scan_shape_valid((int)words, sh))
     return fail(SW_ERR_INVALID_ARGUMENT,
                 "scan shape: tile_rows 32/64/128, warps 4/8/16, tiles_per_super 4/8/16/32, grid_factor 1..64, "
                 "and two tiles per warp within the shared-memory limit");
+  g_last_error.clear();
+  return SW_OK;
+}
+
+int sw_set_scan_shape(sw_context* ctx, uint32_t words, uint32_t size_class, const sw_scan_shape* in) {
+  if (!ctx || !in) return fail(SW_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (words < 1 || words > 8 || size_class >= SW_SCAN_SIZE_CLASSES)
+    return fail(SW_ERR_INVALID_ARGUMENT, "words must be 1..8 and size_class 0..1");
+  const int rc = sw_scan_shape_check(words, in);
+  if (rc != SW_OK) return rc;
+  sw::ScanShape sh;
+  to_shape(*in, sh);
   sw::ScanShapes all = ctx->solver->scan_shapes();
   all.s[words - 1][size_class] = sh;
   set_shapes(ctx, all);

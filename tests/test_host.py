@@ -385,3 +385,28 @@ def test_bench_scan_tuning_uses_held_out_automata():
                 timed_other = {tuple(d) for _, _, d in bench.workload_dfas(name, other)}
                 assert not any(tuple(d) in timed_other for _, _, d in held), (name, rank, other)
             assert not any(tuple(d) in timed for _, _, d in held)
+
+
+def test_scan_shape_rules_on_the_host(native_lib):
+    """The subset check's launch-shape rule (what sw_set_scan_shape accepts),
+    checked without a device: each knob's allowed values, and two tiles per
+    warp within the 200 KiB shared-memory limit."""
+    import synchrowords_gb300 as sw
+    for words in range(1, 9):
+        sw.check_scan_shape(words)  # the default shape fits every width
+        for tr in (32, 64, 128):
+            for warps in (4, 8, 16):
+                fits = 8 * words * tr * 2 * warps <= 200 * 1024
+                if fits:
+                    sw.check_scan_shape(words, tile_rows=tr, warps=warps, tiles_per_super=32, grid_factor=64)
+                else:
+                    with pytest.raises(sw.SynchroError):
+                        sw.check_scan_shape(words, tile_rows=tr, warps=warps)
+    for bad in (dict(tile_rows=48), dict(tile_rows=256), dict(warps=2), dict(warps=32), dict(tiles_per_super=2),
+                dict(tiles_per_super=64), dict(grid_factor=0), dict(grid_factor=65)):
+        with pytest.raises(sw.SynchroError):
+            sw.check_scan_shape(4, **bad)
+    for words in (0, 9):
+        with pytest.raises(sw.SynchroError):
+            sw.check_scan_shape(words)
+    assert native_lib.sw_scan_shape_check(4, None) == -1
